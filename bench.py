@@ -1,0 +1,435 @@
+#!/usr/bin/env python
+"""Benchmark of the QCS state-vector hot path on GB300.
+
+Workload (one "step"): the random brick circuit on 30 qubits, complex64 state
+(8 GiB), depth 40 -- per layer RZ.RY.RZ on every qubit with angles uniform in
+[0, 2 pi), then CNOTs on alternating even/odd neighbour pairs (4180 gates) --
+run from |0...0> through the backend's C ABI.  Two forms: plain per-gate
+kernels and greedy-fused dense blocks.  Metric: gate applications per second
+(original gates / wall time of the step, device-timed with CUDA events on the
+state's stream) and HBM GB/s per sweep type.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Inputs are far larger than L2 (8 GiB state vs 129 MB L2), so no L2 flush is
+needed between steps.  --impl reference times the CPU restatement of the
+reference's algorithm (the oracle, compat mode: out-of-place sweeps, all
+host threads) on a bounded sample of the same 30-qubit workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "30q gate-apps/s & HBM GB/s, fused vs plain, at 1-F<=1e-6 vs FP64 oracle"
+UNIT = "gate-apps/s"
+WORKLOAD = "random brick circuit, 30 qubits, complex64 state (8 GiB), depth 40"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=40)
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--fusion-k", type=int, default=int(os.environ.get("QCS_BENCH_FUSION_K", "5")))
+    ap.add_argument("--engine", default=os.environ.get("QCS_BENCH_ENGINE", "auto"),
+                    choices=["auto", "simt", "tensor"])
+    ap.add_argument("--plain-steps", type=int, default=None,
+                    help="timed steps of the plain form (default: --steps)")
+    ap.add_argument("--parity-qubits", type=int, default=24)
+    ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--cpu-sample-gates", type=int, default=48)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas: one independent state per GPU)
+# ---------------------------------------------------------------------------
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            # pin this rank's GPU before anything touches CUDA
+            os.environ["CUDA_VISIBLE_DEVICES"] = str(self.local)
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+
+REASON_BITS = {0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap",
+               0x8: "hw_slowdown", 0x10: "sync_boost", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown",
+               0x100: "display_clock_setting"}
+
+
+class ClockSampler:
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--id={self.index}",
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 4:
+                try:
+                    self.samples.append((float(parts[0]), float(parts[1]), float(parts[2]),
+                                         int(parts[3], 16)))
+                except ValueError:
+                    pass
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        busy = [s for s in self.samples if not (s[3] & 0x1)] or self.samples
+        reasons = set()
+        for s in busy:
+            for bit, name in REASON_BITS.items():
+                if s[3] & bit:
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(s[0] for s in busy),
+                "sm_max_mhz": max(s[1] for s in busy),
+                "power_w_max": max(s[2] for s in busy),
+                "samples": len(busy), "reasons": sorted(reasons)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(kernel_class: str):
+    """Per-launch DRAM bytes of a kernel class from the committed ncu summary
+    (profiles/traffic.txt: `<class> <bytes per launch> <workload>` lines)."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel_class and not line.startswith("#"):
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle)
+# ---------------------------------------------------------------------------
+
+def mem_available() -> int:
+    """Host MemAvailable in bytes (0 if unknown)."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def cpu_qubits(want: int, buffers: int) -> int:
+    """Largest n <= want whose complex128 oracle state (x buffers) uses at most
+    a third of the available host memory."""
+    avail = mem_available()
+    n = want
+    while n > 16 and (1 << n) * 16 * buffers * 3 > avail:
+        n -= 1
+    return n
+
+
+def infidelity(a, b) -> float:
+    a = a.astype(np.complex128)
+    b = b.astype(np.complex128)
+    return float(1.0 - abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real))
+
+
+def cpu_sample(gates, n: int, count: int, mode: int):
+    """Time the oracle on the first `count` gates of the workload at n qubits.
+    Returns (gate-apps/s, seconds, threads)."""
+    from oracle import oracle as O
+    sub = type(gates)()
+    for k, t, c, a in list(zip(gates.kinds, gates.targets, gates.controls, gates.angles))[:count]:
+        sub.add(k, t, c, a)
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    with O.OracleState(n, mode) as s:
+        t0 = time.perf_counter()
+        s.run(sub)
+        dt = time.perf_counter() - t0
+    return len(sub) / dt, dt, threads
+
+
+def run_reference(args, dist):
+    """--impl reference: the CPU restatement of the reference's algorithm."""
+    if dist.rank != 0:
+        return
+    from oracle import oracle as O
+    from qcs_gb300 import workloads as W
+    O.build()
+    gates = W.brick_circuit(args.qubits, args.depth, args.seed)
+    n_cpu = cpu_qubits(args.qubits, buffers=2)
+    scale = 2.0 ** (n_cpu - args.qubits)
+    count = args.cpu_sample_gates
+    for _ in range(args.warmup):
+        cpu_sample(gates, n_cpu, max(4, count // 8), O.COMPAT)
+    times = []
+    for _ in range(args.steps):
+        rate, dt, threads = cpu_sample(gates, n_cpu, count, O.COMPAT)
+        times.append(dt)
+    dt = sum(times) / len(times)
+    value = count / dt * scale
+    sample = (f"first {count} gates of the {args.qubits}-qubit workload on a {n_cpu}-qubit "
+              f"complex128 state (oracle compat mode = the reference's out-of-place sweep)"
+              + ("" if scale == 1.0 else f", rate scaled by 2^{n_cpu - args.qubits} amplitudes"))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3 * (len(gates) / count) / scale,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "complex128", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "qubits": args.qubits, "depth": args.depth,
+                       "gates": len(gates), "seed": args.seed},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def time_form(state, ops, k, engine, steps, warmup, dist, profile=True):
+    from qcs_gb300 import capi
+    for _ in range(warmup):
+        state.set_basis(0)
+        state.run(ops, fusion_k=k, engine=engine)
+    state.synchronize()
+    if profile:
+        state.profile(True)
+    launches0 = state.launch_count()
+    dist.barrier()
+    state.synchronize()
+    e0 = state.event()
+    for _ in range(steps):
+        state.set_basis(0)
+        state.run(ops, fusion_k=k, engine=engine)
+    e1 = state.event()
+    ms = capi.State.elapsed_ms(e0, e1)
+    state.synchronize()
+    dist.barrier()
+    launches = state.launch_count() - launches0
+    prof = state.profile_read() if profile else {}
+    if profile:
+        state.profile(False)
+    return dist.max(ms), launches, prof
+
+
+def run_ours(args, dist):
+    from qcs_gb300 import build as B
+    from qcs_gb300 import capi
+    from qcs_gb300 import workloads as W
+    B.build()
+    engine = {"auto": capi.FUSE_AUTO, "simt": capi.FUSE_SIMT,
+              "tensor": capi.FUSE_TENSOR}[args.engine]
+    n = args.qubits
+    gates = W.brick_circuit(n, args.depth, args.seed)
+    ops = gates.ops()
+    G = len(gates)
+    state = capi.State(n, capi.C64)
+    peaks = measured_peaks()
+    plain_steps = args.plain_steps if args.plain_steps is not None else args.steps
+
+    with ClockSampler(0) as clk:
+        fused_ms, launches, prof = time_form(state, ops, args.fusion_k, engine, args.steps,
+                                             args.warmup, dist)
+        plain_ms, plain_launches, plain_prof = time_form(state, ops, 0, engine, plain_steps,
+                                                         args.warmup, dist)
+    clocks = clk.summary()
+
+    # end to end through the C ABI with host buffers: gate list from host
+    # memory, 1024 shot draws uploaded, the samples and the argmax read back
+    shots = 1024
+    draws = np.random.default_rng(args.seed).random(shots)
+    for _ in range(1):
+        state.set_basis(0)
+        state.run(ops, fusion_k=args.fusion_k, engine=engine)
+        state.sample(draws)
+    state.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        state.set_basis(0)
+        state.run(ops, fusion_k=args.fusion_k, engine=engine)
+        samples = state.sample(draws)
+        top = state.argmax()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    del samples, top
+
+    world = dist.world
+    value = world * G * args.steps / (fused_ms / 1e3)
+    plain_value = world * G * plain_steps / (plain_ms / 1e3)
+    e2e_value = world * G * args.steps / e2e_s
+
+    # dominant kernel of the fused form
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
+    roof = None
+    if dom:
+        name, (nl, ms, nbytes) = dom
+        achieved = nbytes / (ms / 1e3) / 1e9
+        traffic = ncu_traffic(name)
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                "peak_source": peaks["source"], "traffic": traffic,
+                "algorithmic_bytes_per_launch": nbytes / nl, "launches": nl,
+                "avg_launch_ms": ms / nl}
+    sweep_gbs = {k: {"launches": v[0], "GB/s": v[2] / (v[1] / 1e3) / 1e9,
+                     "share": v[1] / sum(x[1] for x in plain_prof.values())}
+                 for k, v in plain_prof.items()}
+    fused_gbs = {k: {"launches": v[0], "GB/s": v[2] / (v[1] / 1e3) / 1e9,
+                     "share": v[1] / sum(x[1] for x in prof.values())}
+                 for k, v in prof.items()}
+
+    parity = None
+    cpu = None
+    if dist.rank == 0 and not args.no_parity:
+        from oracle import oracle as O
+        O.build()
+        pn = cpu_qubits(args.parity_qubits, buffers=1)
+        pg = W.brick_circuit(pn, args.depth, args.seed)
+        t0 = time.perf_counter()
+        with O.OracleState(pn) as o:
+            o.run(pg)
+            ref = o.amplitudes()
+        cpu_dt = time.perf_counter() - t0
+        threads = os.cpu_count() or 1
+        with capi.State(pn, capi.C64) as s:
+            s.run(pg.ops(), fusion_k=args.fusion_k, engine=engine)
+            a = s.amplitudes()
+        with capi.State(pn, capi.C64) as s:
+            s.run(pg.ops())
+            b = s.amplitudes()
+        parity = {"qubits": pn, "oracle": "FP64 (complex128) CPU oracle, same seed",
+                  "fused": {"infidelity": infidelity(a, ref),
+                            "max_abs_err": float(np.max(np.abs(a - ref)))},
+                  "plain": {"infidelity": infidelity(b, ref),
+                            "max_abs_err": float(np.max(np.abs(b - ref)))}}
+        cpu_rate = len(pg) / cpu_dt * 2.0 ** (pn - n)
+        cpu = {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": (f"oracle (FP64, OpenMP over amplitude pairs) running the full "
+                          f"depth-{args.depth} workload at {pn} qubits in {cpu_dt:.1f} s; "
+                          f"rate scaled to {n} qubits by 2^{pn - n} (cost is linear in "
+                          f"amplitudes)")}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": fused_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "complex64 (fp32 math)",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "qubits": n, "depth": args.depth, "gates": G,
+                   "seed": args.seed, "form": "fused", "fusion_k": args.fusion_k,
+                   "engine": args.engine, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (8 GiB state vs 129 MB), no flush"},
+        "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms / plain_steps,
+                  "steps": plain_steps, "gpu_launches": plain_launches,
+                  "hbm_gbs_by_kernel": sweep_gbs},
+        "fused_over_plain": value / plain_value,
+        "fused_kernels": fused_gbs,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "parity": parity,
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(draws.nbytes),
+                "d2h_bytes_per_step": int(shots * 8 + 8 + 16),
+                "path": "qcs_cuda_set_basis + qcs_cuda_run(host op list) + "
+                        "qcs_cuda_sample(1024 host draws) + qcs_cuda_argmax, host wall clock"},
+        "gpu_launches": launches,
+    }
+    state.close()
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

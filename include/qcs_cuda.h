@@ -1,0 +1,234 @@
+/*
+ * qcs_cuda.h -- C ABI of the GB300 (sm_103a) state-vector backend of QCS.
+ *
+ * This is the boundary a QCS_GPU_CUDA build of the reference calls in place
+ * of its OpenCL backend (SegusFaultise/qcs src/gpu_complex.c) and of the
+ * direct state->vector loops of src/q_gates.c, src/q_utils.c, src/q_state.c
+ * and src/qcs.c.  Plain C types only: no CUDA, C++ or torch types appear in
+ * any signature.  libqcs_gb300.so exports every function declared here, and
+ * also the unchanged public API of include/qcs.h implemented on top of it.
+ *
+ * Conventions
+ *  - Every function returns a status (QCS_CUDA_OK == 0 on success); values
+ *    come back through out-pointers.  qcs_cuda_last_error() gives a message
+ *    for the last failure on the calling thread.
+ *  - A 2x2 gate is 8 doubles: {U00.re, U00.im, U01.re, U01.im, U10.re,
+ *    U10.im, U11.re, U11.im}, the memory layout of t_q_matrix.data in the
+ *    reference (src/internal.h:55-59, data[r*2+c] of struct t_complex), so
+ *    (const double *)gate->data can be passed as is.
+ *  - Qubit q is bit q of the basis index (reference convention,
+ *    src/q_gates.c:28).  Basis indices are 64-bit.
+ *  - Work is queued on the state's own CUDA stream.  Functions that return
+ *    a host value synchronise that stream; the others return immediately.
+ *  - One state must not be used from two threads at once (the reference is
+ *    not reentrant either, src/qcs.c:9-11); distinct states are independent.
+ *  - There is no CPU fallback: without a usable GPU, state creation fails
+ *    with QCS_CUDA_ENODEV.
+ */
+#ifndef QCS_CUDA_H
+#define QCS_CUDA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define QCS_CUDA_OK 0
+#define QCS_CUDA_EINVAL 1   /* bad argument (qubit, index, size, null)   */
+#define QCS_CUDA_ENOMEM 2   /* device or host allocation failed          */
+#define QCS_CUDA_ENODEV 3   /* no usable CUDA device                      */
+#define QCS_CUDA_ELAUNCH 4  /* a kernel launch or CUDA call failed        */
+#define QCS_CUDA_ETIMEOUT 5 /* a bounded device-side wait gave up         */
+#define QCS_CUDA_EUNSUP 6   /* valid but unsupported combination          */
+
+/* ---- state precision -------------------------------------------------- */
+#define QCS_CUDA_C64 0  /* complex64 amplitudes (8 B), FP32 gate math      */
+#define QCS_CUDA_C128 1 /* complex128 amplitudes (16 B), FP64 gate math,
+                           same operation order as the reference          */
+
+/* ---- semantics ---------------------------------------------------------*/
+#define QCS_CUDA_PHYSICAL 0  /* unitary controlled-U, textbook Grover     */
+#define QCS_CUDA_REFERENCE 1 /* the reference's sequential build, bit for
+                                bit: out-of-place sweeps with a buffer swap,
+                                controlled sweep acting as [[U00,U01],[0,1]]
+                                on control=1 pairs (src/q_gates.c:279-291),
+                                stale-buffer phase flip (:311-316) and
+                                mean/|mean| diffusion (:334-355).  Allocates
+                                a second state buffer.                     */
+
+/* ---- gate kinds (struct qcs_cuda_op.kind) ----------------------------- */
+#define QCS_GATE_H 0
+#define QCS_GATE_X 1
+#define QCS_GATE_Y 2
+#define QCS_GATE_Z 3
+#define QCS_GATE_P 4      /* phase, angle                                  */
+#define QCS_GATE_RX 5
+#define QCS_GATE_RY 6
+#define QCS_GATE_RZ 7
+#define QCS_GATE_CNOT 8   /* control, target                               */
+#define QCS_GATE_CPHASE 9 /* control, target, angle (qc_cphase)            */
+#define QCS_GATE_I 10
+#define QCS_OP_PHASE_FLIP 20 /* index                                      */
+#define QCS_OP_DIFFUSION 21
+
+/* One operation of a gate list; 32 bytes, naturally aligned. */
+typedef struct qcs_cuda_op {
+  int kind;
+  int target;
+  int control; /* -1 when unused */
+  int reserved;
+  double angle;
+  long long index; /* basis index for QCS_OP_PHASE_FLIP */
+} qcs_cuda_op;
+
+/* How qcs_cuda_run executes a gate list. */
+typedef struct qcs_cuda_run_options {
+  int fusion_k;  /* 0 or 1: one kernel per gate; 2..7: greedy fusion into
+                    dense blocks of at most fusion_k qubits               */
+  int fusion_engine; /* QCS_FUSE_AUTO, QCS_FUSE_SIMT or QCS_FUSE_TENSOR    */
+  int partitioner;   /* QCS_PARTITION_GREEDY or QCS_PARTITION_LEARNED     */
+  int reserved;
+} qcs_cuda_run_options;
+
+#define QCS_FUSE_AUTO 0
+#define QCS_FUSE_SIMT 1   /* FP32 CUDA-core block kernel (k <= 5)          */
+#define QCS_FUSE_TENSOR 2 /* tcgen05 split-BF16x3 block kernel (k <= 6)    */
+#define QCS_PARTITION_GREEDY 0
+#define QCS_PARTITION_LEARNED 1
+
+typedef struct qcs_cuda_state qcs_cuda_state;
+
+/* ---- library / device --------------------------------------------------*/
+const char *qcs_cuda_strerror(int status);
+const char *qcs_cuda_last_error(void);
+/* Number of visible CUDA devices (0 without a GPU; never fails). */
+int qcs_cuda_device_count(int *count);
+/* Host-side fault injection for tests: make the next `count` device
+ * allocations (what == 1) or kernel launches (what == 2) report failure
+ * without touching the GPU.  what == 0 clears it. */
+int qcs_cuda_debug_inject(int what, int count);
+
+/* ---- state lifecycle ---------------------------------------------------
+ * Replaces q_state_init / q_state_free (src/q_state.c:32-115) and the
+ * OpenCL buffer set-up (src/gpu_complex.c:250-279): the state lives on the
+ * device, initialised to |0...0> (and, in REFERENCE semantics, a zeroed
+ * second buffer). */
+int qcs_cuda_state_create(int num_qubits, int precision, int semantics,
+                          qcs_cuda_state **out);
+int qcs_cuda_state_destroy(qcs_cuda_state *s);
+int qcs_cuda_state_info(const qcs_cuda_state *s, int *num_qubits,
+                        int *precision, int *semantics);
+/* The state's cudaStream_t, as void*. */
+int qcs_cuda_state_stream(qcs_cuda_state *s, void **stream);
+/* Device address of the live amplitude buffer (valid until the next call
+ * that may swap buffers in REFERENCE semantics). */
+int qcs_cuda_state_device_ptr(qcs_cuda_state *s, void **ptr);
+int qcs_cuda_synchronize(qcs_cuda_state *s);
+
+/* q_state_set_basis (src/q_state.c:122-132): live buffer := |index>. */
+int qcs_cuda_set_basis(qcs_cuda_state *s, long long index);
+
+/* Host copies of amplitudes [first, first+count), (re,im) doubles.
+ * read replaces the state->vector reads of q_state_print
+ * (src/q_state.c:145-165). */
+int qcs_cuda_read_amplitudes(qcs_cuda_state *s, long long first,
+                             long long count, double *out);
+int qcs_cuda_write_amplitudes(qcs_cuda_state *s, long long first,
+                              long long count, const double *in);
+
+/* ---- gates ---------------------------------------------------------------
+ * q_apply_1q_gate (src/q_gates.c:25-149; OpenCL q_apply_1q_gate_gpu,
+ * src/gpu_complex.c:521). */
+int qcs_cuda_apply_1q(qcs_cuda_state *s, const double m[8], int target);
+/* q_apply_2q_gate (src/q_gates.c:158-298; OpenCL q_apply_2q_gate_gpu,
+ * src/gpu_complex.c:704): the 2x2 gate on `target` where `control` is 1. */
+int qcs_cuda_apply_controlled_1q(qcs_cuda_state *s, const double m[8],
+                                 int control, int target);
+/* One named gate, built as the qc_<gate> wrappers do
+ * (src/qcs.c:159-228,431-437,485-516; matrices src/q_gates.c:362-491). */
+int qcs_cuda_apply_gate(qcs_cuda_state *s, int kind, int target, int control,
+                        double angle);
+/* Dense 2^k x 2^k block (k <= 7) on an ordered qubit list: bit j of the
+ * block index is qubits[j]; u is row-major (re,im) doubles.  PHYSICAL
+ * semantics only.  No reference counterpart: the reference's only dense
+ * apply is the unused q_gate_apply (src/q_matrix.c:59-96). */
+int qcs_cuda_apply_block(qcs_cuda_state *s, int k, const int *qubits,
+                         const double *u, int engine);
+/* q_apply_phase_flip (src/q_gates.c:305-317). */
+int qcs_cuda_phase_flip(qcs_cuda_state *s, long long index);
+/* q_apply_diffusion (src/q_gates.c:323-356). */
+int qcs_cuda_diffusion(qcs_cuda_state *s);
+/* A whole gate list, optionally fused (options may be NULL: per-gate). */
+int qcs_cuda_run(qcs_cuda_state *s, const qcs_cuda_op *ops, int count,
+                 const qcs_cuda_run_options *options);
+
+/* Host only (no GPU needed): the execution order qcs_cuda_run would use for
+ * ops[0..count) on a num_qubits state with fusion width kmax.  order[j] is
+ * the op applied j-th; item[j] numbers the fused block (or single op) it
+ * belongs to; *num_items receives the number of items.  Both arrays have
+ * `count` entries. */
+int qcs_cuda_plan(const qcs_cuda_op *ops, int count, int num_qubits, int kmax,
+                  int *order, int *item, int *num_items);
+
+/* ---- measurement support (benchmarks) ----------------------------------
+ * Kernel classes for qcs_cuda_profile_read. */
+#define QCS_KCLASS_DENSE1Q 0    /* dense 2x2 sweep                        */
+#define QCS_KCLASS_DIAG1Q 1     /* diagonal 2x2 on every amplitude (RZ)   */
+#define QCS_KCLASS_PHASE_MASK 2 /* phase on amplitudes with bits set      */
+#define QCS_KCLASS_CTRL1Q 3     /* controlled 2x2 (control=1 half)        */
+#define QCS_KCLASS_BLOCK_SIMT 4 /* fused block, CUDA cores                */
+#define QCS_KCLASS_BLOCK_TC 5   /* fused block, tensor cores              */
+#define QCS_KCLASS_REDUCE 6     /* norm / probability / sum reductions    */
+#define QCS_KCLASS_DIFFUSE 7    /* diffusion update (+ fused sum)         */
+#define QCS_KCLASS_COLLAPSE 8   /* measurement collapse, rescale          */
+#define QCS_KCLASS_SAMPLE 9     /* shot sampling                          */
+#define QCS_KCLASS_OTHER 10     /* set-basis, phase flip, finalisers      */
+#define QCS_KCLASS_COUNT 11
+/* enable != 0: from now on bracket every kernel with CUDA events on the
+ * state's stream and accumulate device time and algorithmic bytes per
+ * class (counters are cleared); enable == 0 stops recording. */
+int qcs_cuda_profile_enable(qcs_cuda_state *s, int enable);
+/* Synchronises the stream, then reports class `cls`: launches, total device
+ * milliseconds and algorithmic bytes (any pointer may be NULL). */
+int qcs_cuda_profile_read(qcs_cuda_state *s, int cls, long long *launches,
+                          double *ms, double *bytes);
+/* Kernels launched on this state since it was created. */
+int qcs_cuda_launch_count(qcs_cuda_state *s, long long *count);
+
+/* CUDA events on the state's stream, for device-side timing: record creates
+ * and records one event; elapsed waits for `stop` and returns milliseconds
+ * between the two; destroy frees an event. */
+int qcs_cuda_event_record(qcs_cuda_state *s, void **event);
+int qcs_cuda_event_elapsed(void *start, void *stop, double *ms);
+int qcs_cuda_event_destroy(void *event);
+
+/* ---- reductions and read-out (FP64 accumulation) ----------------------- */
+int qcs_cuda_norm_sq(qcs_cuda_state *s, double *out);
+/* q_state_normalize (src/q_utils.c:44-119): rescale when the norm^2 is
+ * above 1e-12 and not exactly 1. */
+int qcs_cuda_normalize(qcs_cuda_state *s);
+/* Probability of reading 0 on `qubit` (first loop of qc_measure,
+ * src/qcs.c:253-259). */
+int qcs_cuda_prob_zero(qcs_cuda_state *s, int qubit, double *p0);
+/* qc_measure (src/qcs.c:237-284) given the caller's rand()/RAND_MAX draw:
+ * outcome 0 when random_val <= p0; collapse and renormalise. */
+int qcs_cuda_measure(qcs_cuda_state *s, int qubit, double random_val,
+                     int *outcome);
+/* qc_get_probability (src/qcs.c:391-395), 64-bit index. */
+int qcs_cuda_probability(qcs_cuda_state *s, long long index, double *p);
+/* qc_find_most_likely_state (src/qcs.c:464-478): first index of the
+ * largest |amplitude|^2 (0 for an all-zero state); prob may be NULL. */
+int qcs_cuda_argmax(qcs_cuda_state *s, long long *index, double *prob);
+/* <Z_qubit> = P(0) - P(1). */
+int qcs_cuda_expect_z(qcs_cuda_state *s, int qubit, double *out);
+/* Sampling of qc_run_shots (src/qcs.c:584-605): for each draw r in [0,1],
+ * the first index whose running FP64 probability sum exceeds r, or -1 when
+ * r is not below the total.  out_index has `shots` entries. */
+int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
+                    long long *out_index);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

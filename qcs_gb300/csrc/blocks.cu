@@ -1,0 +1,326 @@
+// blocks.cu -- dense k-qubit block application (SIMT engine) and qcs_cuda_run.
+//
+// A block on qubit set Q (k qubits) maps every "column" of the state (one
+// setting of the other n-k qubits) through the 2^k x 2^k matrix U.  A CTA
+// works on tiles of 2^k x 2^c amplitudes: T = Q plus the c lowest qubits
+// outside Q, so every tile is a union of contiguous runs of at least
+// 2^min(7, n-k) amplitudes and its gather/scatter is fully coalesced
+// whatever Q is.  The tile goes through shared memory as S[a][col] (row
+// stride C+1 to spread banks); each thread owns one column and forms
+// out[a'] = sum_a U[a'][a] * S[a][col] with U read from kernel parameters
+// (a uniform, broadcast operand).
+//
+// HBM traffic per block: 2 * N * s bytes (one read, one write), however many
+// gates the block holds.  FP32 work: 8 * 2^k flops per amplitude, so this
+// engine stays bandwidth-bound up to k = 4 on GB300's CUDA cores; larger
+// blocks belong on the tensor cores (blocks_tc.cu).
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "fusion.h"
+
+namespace qcs {
+
+int apply_1q(qcs_cuda_state *s, const double m[8], int t);
+int apply_ctrl(qcs_cuda_state *s, const double m[8], int c, int t);
+int phase_flip(qcs_cuda_state *s, i64 index);
+int diffusion(qcs_cuda_state *s);
+int check_qubit(const qcs_cuda_state *s, int q, const char *what);
+int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u);
+bool tc_supported(const qcs_cuda_state *s, int k);
+
+constexpr int kBlockThreads = 128;  // = max columns per tile
+constexpr int kMaxColBits = 7;
+constexpr int kSimtMaxK = 5;
+
+// Tile geometry, computed on the host.  Local index l of a tile has nT bits;
+// bit m stands for qubit tq[m] (ascending).  l = lo | hi << 6 and every
+// per-element quantity is a sum of a lo-table and a hi-table entry.
+struct TileGeom {
+  int n, k, c, nT;
+  i64 n_tiles;
+  int nfree;
+  signed char freeq[40];  // qubits outside T, ascending (tile id bits)
+  i64 goff_lo[64];
+  i64 goff_hi[64];
+  unsigned char a_lo[64], a_hi[64];
+  unsigned char col_lo[64], col_hi[64];
+};
+
+template <typename C, int K> struct BlockU { C u[K * K]; };
+
+template <typename C, int K>
+__global__ void __launch_bounds__(kBlockThreads)
+    k_block_simt(C *v, const TileGeom g, const BlockU<C, K> U) {
+  const int Cn = 1 << g.c;        // columns per tile
+  const int stride = Cn + 1;      // smem row stride (elements)
+  const int L = 1 << g.nT;        // elements per tile
+  extern __shared__ unsigned char smem_raw[];
+  C *S = reinterpret_cast<C *>(smem_raw);
+  const int tid = threadIdx.x;
+  for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x) {
+    i64 base = 0;
+    for (int j = 0; j < g.nfree; j++) base |= ((tile >> j) & 1LL) << g.freeq[j];
+    // gather (global order, coalesced)
+    for (int l = tid; l < L; l += kBlockThreads) {
+      int lo = l & 63, hi = l >> 6;
+      i64 off = g.goff_lo[lo] + g.goff_hi[hi];
+      int a = g.a_lo[lo] + g.a_hi[hi];
+      int col = g.col_lo[lo] + g.col_hi[hi];
+      S[a * stride + col] = v[base + off];
+    }
+    __syncthreads();
+    if (tid < Cn) {
+      C in[K];
+#pragma unroll
+      for (int a = 0; a < K; a++) in[a] = S[a * stride + tid];
+#pragma unroll
+      for (int r = 0; r < K; r++) {
+        C acc = cmul(U.u[r * K], in[0]);
+#pragma unroll
+        for (int a = 1; a < K; a++) acc = cadd(acc, cmul(U.u[r * K + a], in[a]));
+        S[r * stride + tid] = acc;
+      }
+    }
+    __syncthreads();
+    for (int l = tid; l < L; l += kBlockThreads) {
+      int lo = l & 63, hi = l >> 6;
+      i64 off = g.goff_lo[lo] + g.goff_hi[hi];
+      int a = g.a_lo[lo] + g.a_hi[hi];
+      int col = g.col_lo[lo] + g.col_hi[hi];
+      v[base + off] = S[a * stride + col];
+    }
+    __syncthreads();
+  }
+}
+
+// qubits[] in caller order (bit j of the block index is qubits[j]).
+static void make_geom(const qcs_cuda_state *s, int k, const int *qubits, TileGeom &g) {
+  memset(&g, 0, sizeof(g));
+  g.n = s->n;
+  g.k = k;
+  int c = s->n - k < kMaxColBits ? s->n - k : kMaxColBits;
+  g.c = c;
+  g.nT = k + c;
+  std::vector<int> role(s->n, -1);  // -1 free, >=0 block bit, -2 column
+  for (int j = 0; j < k; j++) role[qubits[j]] = j;
+  int taken = 0;
+  for (int q = 0; q < s->n && taken < c; q++)
+    if (role[q] == -1) { role[q] = -2; taken++; }
+  std::vector<int> tq;
+  for (int q = 0; q < s->n; q++) {
+    if (role[q] == -1) g.freeq[g.nfree++] = (signed char)q;
+    else tq.push_back(q);
+  }
+  g.n_tiles = 1LL << g.nfree;
+  // per T position: global offset bit, block bit, column bit
+  std::vector<i64> gbit(g.nT);
+  std::vector<int> abit(g.nT, 0), cbit(g.nT, 0);
+  int colj = 0;
+  for (int m = 0; m < g.nT; m++) {
+    int q = tq[m];
+    gbit[m] = 1LL << q;
+    if (role[q] >= 0) abit[m] = 1 << role[q];
+    else cbit[m] = 1 << (colj++);
+  }
+  for (int e = 0; e < 64; e++) {
+    i64 go = 0, gh = 0;
+    int al = 0, ah = 0, cl = 0, ch = 0;
+    for (int m = 0; m < g.nT; m++) {
+      if (m < 6) {
+        if ((e >> m) & 1) { go += gbit[m]; al += abit[m]; cl += cbit[m]; }
+      } else {
+        if ((e >> (m - 6)) & 1) { gh += gbit[m]; ah += abit[m]; ch += cbit[m]; }
+      }
+    }
+    g.goff_lo[e] = go;
+    g.goff_hi[e] = gh;
+    g.a_lo[e] = (unsigned char)al;
+    g.a_hi[e] = (unsigned char)ah;
+    g.col_lo[e] = (unsigned char)cl;
+    g.col_hi[e] = (unsigned char)ch;
+  }
+}
+
+template <typename C, int K>
+static int launch_block(qcs_cuda_state *s, const TileGeom &g, const double *u) {
+  BlockU<C, K> U;
+  for (int i = 0; i < K * K; i++) U.u[i] = make_c<C>(u[2 * i], u[2 * i + 1]);
+  size_t smem = (size_t)K * ((1 << g.c) + 1) * sizeof(C);
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_block_simt<C, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         96 * 1024);
+    configured = true;
+  }
+  i64 want = g.n_tiles;
+  i64 cap = (i64)s->dev.num_sms * 8;
+  int grid = (int)(want < cap ? want : cap);
+  prof_begin(s);
+  k_block_simt<C, K><<<grid, kBlockThreads, smem, s->stream>>>((C *)s->vec, g, U);
+  return launched(s, KC_BLOCK_SIMT, 2.0 * s->size * sizeof(C), "apply_block (SIMT)");
+}
+
+template <typename C>
+static int apply_block_simt_t(qcs_cuda_state *s, int k, const int *qubits, const double *u) {
+  TileGeom g;
+  make_geom(s, k, qubits, g);
+  switch (k) {
+    case 1: return launch_block<C, 2>(s, g, u);
+    case 2: return launch_block<C, 4>(s, g, u);
+    case 3: return launch_block<C, 8>(s, g, u);
+    case 4: return launch_block<C, 16>(s, g, u);
+    case 5: return launch_block<C, 32>(s, g, u);
+    default: return set_error(QCS_CUDA_EUNSUP, "SIMT block engine supports k <= %d", kSimtMaxK);
+  }
+}
+
+int apply_block(qcs_cuda_state *s, int k, const int *qubits, const double *u, int engine) {
+  invalidate_sum(s);
+  bool want_tc = engine == QCS_FUSE_TENSOR ||
+                 (engine == QCS_FUSE_AUTO && k > 4 && tc_supported(s, k));
+  if (want_tc) {
+    if (!tc_supported(s, k))
+      return set_error(QCS_CUDA_EUNSUP, "tensor-core block engine: unsupported k=%d / precision", k);
+    return apply_block_tc(s, k, qubits, u);
+  }
+  if (s->prec == QCS_CUDA_C128) return apply_block_simt_t<double2>(s, k, qubits, u);
+  return apply_block_simt_t<float2>(s, k, qubits, u);
+}
+
+static int validate_ops(const qcs_cuda_state *s, const qcs_cuda_op *ops, int count) {
+  for (int i = 0; i < count; i++) {
+    const qcs_cuda_op &o = ops[i];
+    if (o.kind == QCS_OP_DIFFUSION) continue;
+    if (o.kind == QCS_OP_PHASE_FLIP) {
+      if (o.index < 0 || o.index >= s->size)
+        return set_error(QCS_CUDA_EINVAL, "op %d: phase flip index %lld out of range", i, o.index);
+      continue;
+    }
+    if (!gate_kind_valid(o.kind)) return set_error(QCS_CUDA_EINVAL, "op %d: unknown kind %d", i, o.kind);
+    if (o.target < 0 || o.target >= s->n)
+      return set_error(QCS_CUDA_EINVAL, "op %d: target %d out of range", i, o.target);
+    if (gate_is_controlled(o.kind) &&
+        (o.control < 0 || o.control >= s->n || o.control == o.target))
+      return set_error(QCS_CUDA_EINVAL, "op %d: bad control %d", i, o.control);
+  }
+  return QCS_CUDA_OK;
+}
+
+static int apply_op(qcs_cuda_state *s, const qcs_cuda_op &o) {
+  if (o.kind == QCS_OP_PHASE_FLIP) return phase_flip(s, o.index);
+  if (o.kind == QCS_OP_DIFFUSION) return diffusion(s);
+  double m[8];
+  gate_matrix(o.kind, o.angle, m);
+  if (gate_is_controlled(o.kind)) return apply_ctrl(s, m, o.control, o.target);
+  return apply_1q(s, m, o.target);
+}
+
+int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda_run_options *opt) {
+  int rc = validate_ops(s, ops, count);
+  if (rc) return rc;
+  int k = opt ? opt->fusion_k : 0;
+  if (k <= 1 || s->sem == QCS_CUDA_REFERENCE) {
+    for (int i = 0; i < count; i++) {
+      rc = apply_op(s, ops[i]);
+      if (rc) return rc;
+    }
+    return QCS_CUDA_OK;
+  }
+  if (k > 7) k = 7;
+  int engine = opt->fusion_engine;
+  int kcap = engine == QCS_FUSE_SIMT ? kSimtMaxK : 7;
+  if (k > kcap) k = kcap;
+  if (k > s->n) k = s->n;
+  PartitionOptions po;
+  po.kmax = k;
+  po.cost = nullptr;
+  po.cost_ctx = nullptr;
+  std::vector<PlanItem> plan = partition(ops, count, s->n, po);
+  std::vector<cd> u;
+  for (const PlanItem &it : plan) {
+    if (it.kind == 1) {
+      rc = apply_op(s, ops[it.op]);
+    } else if (it.gates.size() == 1) {
+      rc = apply_op(s, ops[it.gates[0]]);
+    } else {
+      block_matrix(ops, it, u);
+      const int kb = (int)it.qubits.size();
+      if (kb == 1) {
+        double m[8] = {u[0].real(), u[0].imag(), u[1].real(), u[1].imag(),
+                       u[2].real(), u[2].imag(), u[3].real(), u[3].imag()};
+        rc = apply_1q(s, m, it.qubits[0]);
+      } else {
+        rc = apply_block(s, kb, it.qubits.data(), reinterpret_cast<const double *>(u.data()), engine);
+      }
+    }
+    if (rc) return rc;
+  }
+  return QCS_CUDA_OK;
+}
+
+}  // namespace qcs
+
+using namespace qcs;
+
+extern "C" {
+
+int qcs_cuda_apply_block(qcs_cuda_state *s, int k, const int *qubits, const double *u,
+                         int engine) {
+  QCS_CHECK_STATE(s);
+  if (!qubits || !u) return set_error(QCS_CUDA_EINVAL, "null block argument");
+  if (k < 1 || k > 7 || k > s->n) return set_error(QCS_CUDA_EINVAL, "block size k=%d unsupported", k);
+  if (s->sem == QCS_CUDA_REFERENCE)
+    return set_error(QCS_CUDA_EUNSUP, "dense blocks need PHYSICAL semantics");
+  i64 seen = 0;
+  for (int j = 0; j < k; j++) {
+    int rc = check_qubit(s, qubits[j], "apply_block");
+    if (rc) return rc;
+    if (seen & (1LL << qubits[j])) return set_error(QCS_CUDA_EINVAL, "repeated qubit %d", qubits[j]);
+    seen |= 1LL << qubits[j];
+  }
+  return apply_block(s, k, qubits, u, engine);
+}
+
+int qcs_cuda_plan(const qcs_cuda_op *ops, int count, int num_qubits, int kmax, int *order,
+                  int *item, int *num_items) {
+  if (count < 0 || (count > 0 && (!ops || !order || !item)) || !num_items)
+    return set_error(QCS_CUDA_EINVAL, "bad plan arguments");
+  if (num_qubits < 1 || num_qubits > 36) return set_error(QCS_CUDA_EINVAL, "bad qubit count");
+  qcs_cuda_state shape;
+  memset(&shape, 0, sizeof(shape));
+  shape.n = num_qubits;
+  shape.size = 1LL << num_qubits;
+  int rc = validate_ops(&shape, ops, count);
+  if (rc) return rc;
+  PartitionOptions po;
+  po.kmax = kmax < 1 ? 1 : (kmax > 7 ? 7 : kmax);
+  po.cost = nullptr;
+  po.cost_ctx = nullptr;
+  std::vector<PlanItem> plan = partition(ops, count, num_qubits, po);
+  int j = 0;
+  for (size_t it = 0; it < plan.size(); it++) {
+    if (plan[it].kind == 1) {
+      order[j] = plan[it].op;
+      item[j++] = (int)it;
+    } else {
+      for (int g : plan[it].gates) {
+        order[j] = g;
+        item[j++] = (int)it;
+      }
+    }
+  }
+  *num_items = (int)plan.size();
+  return QCS_CUDA_OK;
+}
+
+int qcs_cuda_run(qcs_cuda_state *s, const qcs_cuda_op *ops, int count,
+                 const qcs_cuda_run_options *options) {
+  QCS_CHECK_STATE(s);
+  if (count < 0 || (count > 0 && !ops)) return set_error(QCS_CUDA_EINVAL, "bad op list");
+  return run_ops(s, ops, count, options);
+}
+
+}  // extern "C"

@@ -1,0 +1,362 @@
+// gates.cu -- per-gate amplitude sweeps (the plain path).
+//
+// The reference applies every gate as a full out-of-place sweep plus a copy
+// (src/q_gates.c:131-148, :277-297).  Here PHYSICAL semantics sweep in
+// place and touch only the amplitudes a gate changes:
+//
+//   dense 1q (H, X, Y, RX, RY)      all pairs (lo, lo + 2^t)       2*N*s bytes
+//   diagonal 1q with U00 == 1 (Z,P) amplitudes with bit t set        N*s
+//   diagonal 1q (RZ)                all amplitudes, no pairing     2*N*s
+//   controlled 2x2 (CNOT)           pairs with the control bit set   N*s
+//   controlled diagonal (CPHASE)    amplitudes with both bits set   N*s/2
+//
+// REFERENCE semantics keep the reference's out-of-place sweeps, the buffer
+// swap and the [[U00,U01],[0,1]] controlled rule so that results match its
+// sequential build bit for bit in complex128.
+//
+// All kernels are grid-stride loops over 64-bit indices; each thread keeps
+// kUnroll independent pairs in flight to cover HBM latency.
+#include "common.cuh"
+
+namespace qcs {
+
+constexpr int kUnroll = 4;
+constexpr int kSweepBlocksPerSM = 8;
+
+// Dense 2x2 on every pair (lo, lo + 2^t).  OOP selects dst != src (REFERENCE
+// semantics); in place otherwise.  Output per pair is exactly
+// c_add(c_mul(g0,v0), c_mul(g1,v1)), c_add(c_mul(g2,v0), c_mul(g3,v1)).
+template <typename C>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_dense1q(C *dst, const C *src, i64 npairs, int t, Mat2<C> m) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  const i64 tb = 1LL << t;
+  i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p + (kUnroll - 1) * nthr < npairs; p += kUnroll * nthr) {
+    C v0[kUnroll], v1[kUnroll];
+    i64 lo[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      lo[u] = insert_zero(p + u * nthr, t);
+      v0[u] = src[lo[u]];
+      v1[u] = src[lo[u] + tb];
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      dst[lo[u]] = cadd(cmul(m.g[0], v0[u]), cmul(m.g[1], v1[u]));
+      dst[lo[u] + tb] = cadd(cmul(m.g[2], v0[u]), cmul(m.g[3], v1[u]));
+    }
+  }
+  for (; p < npairs; p += nthr) {
+    i64 lo = insert_zero(p, t);
+    C v0 = src[lo], v1 = src[lo + tb];
+    dst[lo] = cadd(cmul(m.g[0], v0), cmul(m.g[1], v1));
+    dst[lo + tb] = cadd(cmul(m.g[2], v0), cmul(m.g[3], v1));
+  }
+}
+
+// diag(d0, d1) on every amplitude: psi_i *= d_{bit t of i}.  Equal to the
+// dense formula (the off-diagonal products are +-0).
+template <typename C>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_diag1q(C *v, i64 size, int t, C d0, C d1) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + (kUnroll - 1) * nthr < size; i += kUnroll * nthr) {
+    C a[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) a[u] = v[i + u * nthr];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      i64 j = i + u * nthr;
+      v[j] = cmul(((j >> t) & 1) ? d1 : d0, a[u]);
+    }
+  }
+  for (; i < size; i += nthr) v[i] = cmul(((i >> t) & 1) ? d1 : d0, v[i]);
+}
+
+// psi_i *= phase for every i whose bits b0 and b1 are both set (b1 < 0: only
+// b0).  Z, P (b1 < 0) and CPHASE (control, target).
+template <typename C>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_phase_mask(C *v, i64 count, int blo, int bhi, i64 setmask, C phase) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p + (kUnroll - 1) * nthr < count; p += kUnroll * nthr) {
+    C a[kUnroll];
+    i64 idx[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      i64 x = insert_zero(p + u * nthr, blo);
+      if (bhi >= 0) x = insert_zero(x, bhi);
+      idx[u] = x | setmask;
+      a[u] = v[idx[u]];
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) v[idx[u]] = cmul(phase, a[u]);
+  }
+  for (; p < count; p += nthr) {
+    i64 x = insert_zero(p, blo);
+    if (bhi >= 0) x = insert_zero(x, bhi);
+    x |= setmask;
+    v[x] = cmul(phase, v[x]);
+  }
+}
+
+// Unitary controlled-U, in place: pairs (lo, lo + 2^t) whose control bit is
+// set.  lo enumerates indices with bit c = 1 and bit t = 0.
+template <typename C>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_ctrl1q(C *v, i64 npairs, int blo, int bhi, i64 cmask, int t, Mat2<C> m) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  const i64 tb = 1LL << t;
+  i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p + (kUnroll - 1) * nthr < npairs; p += kUnroll * nthr) {
+    C v0[kUnroll], v1[kUnroll];
+    i64 lo[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      lo[u] = insert_zero(insert_zero(p + u * nthr, blo), bhi) | cmask;
+      v0[u] = v[lo[u]];
+      v1[u] = v[lo[u] + tb];
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      v[lo[u]] = cadd(cmul(m.g[0], v0[u]), cmul(m.g[1], v1[u]));
+      v[lo[u] + tb] = cadd(cmul(m.g[2], v0[u]), cmul(m.g[3], v1[u]));
+    }
+  }
+  for (; p < npairs; p += nthr) {
+    i64 lo = insert_zero(insert_zero(p, blo), bhi) | cmask;
+    C v0 = v[lo], v1 = v[lo + tb];
+    v[lo] = cadd(cmul(m.g[0], v0), cmul(m.g[1], v1));
+    v[lo + tb] = cadd(cmul(m.g[2], v0), cmul(m.g[3], v1));
+  }
+}
+
+// The reference's controlled sweep (src/q_gates.c:277-297), out of place:
+// every pair is copied, except that control=1 pairs get
+// lo := c_add(c_mul(g0,v0), c_mul(g1,v1)) and keep hi := v1.
+template <typename C>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_ctrl1q_reference(C *dst, const C *src, i64 npairs, int t, i64 cmask, Mat2<C> m) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  const i64 tb = 1LL << t;
+  for (i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += nthr) {
+    i64 lo = insert_zero(p, t);
+    C v0 = src[lo], v1 = src[lo + tb];
+    dst[lo] = (lo & cmask) ? cadd(cmul(m.g[0], v0), cmul(m.g[1], v1)) : v0;
+    dst[lo + tb] = v1;
+  }
+}
+
+// Phase flip on one amplitude.  PHYSICAL: in place; also keeps the cached
+// amplitude sum (sum[0..1]) in step when `sum` is non-null.  REFERENCE: the
+// host has already swapped buffers, so dst is the stale buffer and the value
+// comes from the current one (src/q_gates.c:311-316).
+template <typename C>
+__global__ void k_flip(C *dst, const C *src, i64 index, double *sum) {
+  C a = src[index];
+  dst[index] = make_c<C>(-(double)a.x, -(double)a.y);
+  if (sum) {
+    sum[0] -= 2.0 * (double)a.x;
+    sum[1] -= 2.0 * (double)a.y;
+  }
+}
+
+static bool is_zero(const double *z) { return z[0] == 0.0 && z[1] == 0.0; }
+static bool is_one(const double *z) { return z[0] == 1.0 && z[1] == 0.0; }
+
+static void swap_buffers(qcs_cuda_state *s) {
+  void *t = s->vec;
+  s->vec = s->scratch;
+  s->scratch = t;
+}
+
+template <typename C>
+static int apply_1q_t(qcs_cuda_state *s, const double m[8], int t) {
+  const DeviceInfo &d = s->dev;
+  const double Ns = (double)s->size * sizeof(C);
+  Mat2<C> g = to_mat2<C>(m);
+  C *v = (C *)s->vec;
+  if (s->sem == QCS_CUDA_REFERENCE) {
+    i64 np = s->size / 2;
+    prof_begin(s);
+    k_dense1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads, 0,
+                   s->stream>>>((C *)s->scratch, v, np, t, g);
+    int rc = launched(s, KC_DENSE1Q, 2 * Ns, "apply_1q");
+    if (rc) return rc;
+    swap_buffers(s);
+    return QCS_CUDA_OK;
+  }
+  bool diag = is_zero(m + 2) && is_zero(m + 4);
+  if (diag && is_one(m)) {
+    if (is_one(m + 6)) return QCS_CUDA_OK;  // identity: 1*v + 0*v == v
+    i64 cnt = s->size / 2;
+    prof_begin(s);
+    k_phase_mask<C><<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads,
+                      0, s->stream>>>(v, cnt, t, -1, 1LL << t, g.g[3]);
+    return launched(s, KC_PHASE_MASK, Ns, "apply_1q (phase)");
+  }
+  if (diag) {
+    prof_begin(s);
+    k_diag1q<C><<<grid_for(s->size, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads,
+                  0, s->stream>>>(v, s->size, t, g.g[0], g.g[3]);
+    return launched(s, KC_DIAG1Q, 2 * Ns, "apply_1q (diagonal)");
+  }
+  i64 np = s->size / 2;
+  prof_begin(s);
+  k_dense1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads, 0,
+                 s->stream>>>(v, v, np, t, g);
+  return launched(s, KC_DENSE1Q, 2 * Ns, "apply_1q");
+}
+
+template <typename C>
+static int apply_ctrl_t(qcs_cuda_state *s, const double m[8], int c, int t) {
+  const DeviceInfo &d = s->dev;
+  const double Ns = (double)s->size * sizeof(C);
+  Mat2<C> g = to_mat2<C>(m);
+  C *v = (C *)s->vec;
+  i64 cmask = 1LL << c;
+  if (s->sem == QCS_CUDA_REFERENCE) {
+    i64 np = s->size / 2;
+    prof_begin(s);
+    k_ctrl1q_reference<C><<<grid_for(np, kSweepThreads, d, kSweepBlocksPerSM), kSweepThreads, 0,
+                            s->stream>>>((C *)s->scratch, v, np, t, cmask, g);
+    int rc = launched(s, KC_CTRL1Q, 2 * Ns, "apply_controlled");
+    if (rc) return rc;
+    swap_buffers(s);
+    return QCS_CUDA_OK;
+  }
+  int blo = c < t ? c : t, bhi = c < t ? t : c;
+  bool diag = is_zero(m + 2) && is_zero(m + 4);
+  if (diag && is_one(m)) {
+    if (is_one(m + 6)) return QCS_CUDA_OK;
+    i64 cnt = s->size / 4;
+    prof_begin(s);
+    k_phase_mask<C><<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads,
+                      0, s->stream>>>(v, cnt, blo, bhi, cmask | (1LL << t), g.g[3]);
+    return launched(s, KC_PHASE_MASK, Ns / 2, "apply_controlled (phase)");
+  }
+  i64 np = s->size / 4;
+  prof_begin(s);
+  k_ctrl1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads, 0,
+                s->stream>>>(v, np, blo, bhi, cmask, t, g);
+  return launched(s, KC_CTRL1Q, Ns, "apply_controlled");
+}
+
+int apply_1q(qcs_cuda_state *s, const double m[8], int t) {
+  invalidate_sum(s);
+  return s->prec == QCS_CUDA_C128 ? apply_1q_t<double2>(s, m, t) : apply_1q_t<float2>(s, m, t);
+}
+
+int apply_ctrl(qcs_cuda_state *s, const double m[8], int c, int t) {
+  invalidate_sum(s);
+  return s->prec == QCS_CUDA_C128 ? apply_ctrl_t<double2>(s, m, c, t)
+                                  : apply_ctrl_t<float2>(s, m, c, t);
+}
+
+int phase_flip(qcs_cuda_state *s, i64 index) {
+  void *src = s->vec;
+  void *dst = s->vec;
+  double *sum = nullptr;
+  if (s->sem == QCS_CUDA_REFERENCE) {
+    swap_buffers(s);
+    dst = s->vec;  // the stale buffer becomes live
+  } else if (s->sum_valid) {
+    sum = s->d_result + 4;
+  }
+  prof_begin(s);
+  if (s->prec == QCS_CUDA_C128)
+    k_flip<double2><<<1, 1, 0, s->stream>>>((double2 *)dst, (const double2 *)src, index, sum);
+  else
+    k_flip<float2><<<1, 1, 0, s->stream>>>((float2 *)dst, (const float2 *)src, index, sum);
+  if (s->sem == QCS_CUDA_REFERENCE) invalidate_sum(s);
+  return launched(s, KC_OTHER, s->prec == QCS_CUDA_C128 ? 32.0 : 16.0, "phase_flip");
+}
+
+// Gate matrices of the qc_<gate> wrappers (src/q_gates.c:362-491), built on
+// the host in FP64 with the same libm calls.
+void gate_matrix(int kind, double angle, double m[8]) {
+  for (int i = 0; i < 8; i++) m[i] = 0.0;
+  double ch, sh;
+  switch (kind) {
+    case QCS_GATE_X:
+    case QCS_GATE_CNOT:
+      m[2] = 1.0; m[4] = 1.0; break;
+    case QCS_GATE_H: {
+      double h = 1.0 / sqrt(2.0);
+      m[0] = h; m[2] = h; m[4] = h; m[6] = -h; break;
+    }
+    case QCS_GATE_Y:
+      m[3] = -1.0; m[5] = 1.0; break;
+    case QCS_GATE_Z:
+      m[0] = 1.0; m[6] = -1.0; break;
+    case QCS_GATE_P:
+    case QCS_GATE_CPHASE:
+      m[0] = 1.0; m[6] = cos(angle); m[7] = sin(angle); break;
+    case QCS_GATE_RX:
+      ch = cos(angle / 2.0); sh = sin(angle / 2.0);
+      m[0] = ch; m[3] = -sh; m[5] = -sh; m[6] = ch; break;
+    case QCS_GATE_RY:
+      ch = cos(angle / 2.0); sh = sin(angle / 2.0);
+      m[0] = ch; m[2] = -sh; m[4] = sh; m[6] = ch; break;
+    case QCS_GATE_RZ:
+      ch = cos(angle / 2.0); sh = sin(angle / 2.0);
+      m[0] = ch; m[1] = -sh; m[6] = ch; m[7] = sh; break;
+    default:  // identity
+      m[0] = 1.0; m[6] = 1.0; break;
+  }
+}
+
+bool gate_is_controlled(int kind) { return kind == QCS_GATE_CNOT || kind == QCS_GATE_CPHASE; }
+
+bool gate_kind_valid(int kind) { return kind >= QCS_GATE_H && kind <= QCS_GATE_I; }
+
+int check_qubit(const qcs_cuda_state *s, int q, const char *what) {
+  if (q < 0 || q >= s->n)
+    return set_error(QCS_CUDA_EINVAL, "%s: qubit %d outside [0, %d)", what, q, s->n);
+  return QCS_CUDA_OK;
+}
+
+}  // namespace qcs
+
+using namespace qcs;
+
+extern "C" {
+
+int qcs_cuda_apply_1q(qcs_cuda_state *s, const double m[8], int target) {
+  QCS_CHECK_STATE(s);
+  if (!m) return set_error(QCS_CUDA_EINVAL, "null gate matrix");
+  int rc = check_qubit(s, target, "apply_1q");
+  return rc ? rc : apply_1q(s, m, target);
+}
+
+int qcs_cuda_apply_controlled_1q(qcs_cuda_state *s, const double m[8], int control,
+                                 int target) {
+  QCS_CHECK_STATE(s);
+  if (!m) return set_error(QCS_CUDA_EINVAL, "null gate matrix");
+  int rc = check_qubit(s, control, "apply_controlled");
+  if (!rc) rc = check_qubit(s, target, "apply_controlled");
+  if (rc) return rc;
+  if (control == target) return set_error(QCS_CUDA_EINVAL, "control equals target (%d)", target);
+  return apply_ctrl(s, m, control, target);
+}
+
+int qcs_cuda_apply_gate(qcs_cuda_state *s, int kind, int target, int control, double angle) {
+  QCS_CHECK_STATE(s);
+  if (!gate_kind_valid(kind)) return set_error(QCS_CUDA_EINVAL, "unknown gate kind %d", kind);
+  double m[8];
+  gate_matrix(kind, angle, m);
+  if (gate_is_controlled(kind)) return qcs_cuda_apply_controlled_1q(s, m, control, target);
+  return qcs_cuda_apply_1q(s, m, target);
+}
+
+int qcs_cuda_phase_flip(qcs_cuda_state *s, long long index) {
+  QCS_CHECK_STATE(s);
+  if (index < 0 || index >= s->size)
+    return set_error(QCS_CUDA_EINVAL, "phase flip index %lld outside [0, %lld)", index, s->size);
+  return phase_flip(s, index);
+}
+
+}  // extern "C"

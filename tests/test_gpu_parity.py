@@ -1,0 +1,383 @@
+"""Parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Bars:
+  * complex128 gate sweeps: bit-exact -- against the reference's own
+    sequential build (golden fixtures, REFERENCE semantics) and against the
+    oracle (PHYSICAL semantics);
+  * complex64: max |delta| <= 2e-5 and infidelity <= 1e-9 against the FP64
+    oracle on the same inputs (FP32 rounding only);
+  * integer answers (argmax, sample indices, measurement outcomes):
+    identical.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from qcs_gb300 import capi
+from qcs_gb300 import workloads as W
+from tests.helpers import bits_equal, gates_from, infidelity
+
+pytestmark = pytest.mark.gpu
+
+C64_ATOL = 2e-5
+C64_INFID = 1e-9
+
+
+def oracle_state(n, gates, mode=O.PHYSICAL):
+    s = O.OracleState(n, mode)
+    s.run(gates)
+    return s
+
+
+# ---- complex128: bit-exact ---------------------------------------------------
+
+@pytest.mark.parametrize("name", ["ref_1q_n10", "ref_mixed_n10_s0", "ref_mixed_n10_s1",
+                                  "ref_random_n12"])
+def test_c128_reference_semantics_bitexact_vs_reference_build(golden, name):
+    d = golden(name)
+    n = int(d["n"])
+    with capi.State(n, capi.C128, capi.REFERENCE) as s:
+        s.run(gates_from(d))
+        assert bits_equal(s.amplitudes(), d["ref"])
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_c128_physical_bitexact_vs_oracle(seed):
+    n = 13
+    basis, g = W.random_circuit(n, seed, 200)
+    full = W.basis_gates(n, basis)
+    full.extend(g)
+    with capi.State(n, capi.C128) as s, oracle_state(n, full) as o:
+        s.run(full)
+        assert bits_equal(s.amplitudes(), o.amplitudes())
+
+
+def test_c128_physical_matches_numpy_golden(golden):
+    d = golden("ref_random_n12")
+    with capi.State(12, capi.C128) as s:
+        s.run(gates_from(d))
+        np.testing.assert_allclose(s.amplitudes(), d["physical"], atol=1e-12)
+
+
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_every_gate_every_qubit(prec):
+    n = 6
+    rng = np.random.default_rng(1)
+    init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    init /= np.linalg.norm(init)
+    for kind in (W.H, W.X, W.Y, W.Z, W.P, W.RX, W.RY, W.RZ, W.CNOT, W.CPHASE):
+        for t in range(n):
+            ctrls = [c for c in range(n) if c != t] if kind in (W.CNOT, W.CPHASE) else [-1]
+            for c in ctrls:
+                ang = 0.3 + 0.7 * t + 0.11 * c
+                with capi.State(n, prec) as s, O.OracleState(n) as o:
+                    s.set_amplitudes(init)
+                    o.set_amplitudes(init)
+                    s.apply_gate(kind, t, c, ang)
+                    o.apply_gate(kind, t, c, ang)
+                    if prec == capi.C128:
+                        assert bits_equal(s.amplitudes(), o.amplitudes()), (kind, t, c)
+                    else:
+                        np.testing.assert_allclose(s.amplitudes(), o.amplitudes(), atol=1e-6)
+
+
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_reference_semantics_controlled_rule(prec):
+    """REFERENCE semantics reproduce [[U00,U01],[0,1]] on control=1 pairs."""
+    n = 7
+    rng = np.random.default_rng(3)
+    init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    for kind, c, t in ((W.CNOT, 0, 3), (W.CNOT, 5, 1), (W.CPHASE, 2, 6)):
+        with capi.State(n, prec, capi.REFERENCE) as s, O.OracleState(n, O.COMPAT) as o:
+            s.set_amplitudes(init)
+            o.set_amplitudes(init)
+            s.apply_gate(kind, t, c, 0.7)
+            o.apply_gate(kind, t, c, 0.7)
+            if prec == capi.C128:
+                assert bits_equal(s.amplitudes(), o.amplitudes())
+            else:
+                np.testing.assert_allclose(s.amplitudes(), o.amplitudes(), atol=1e-5)
+
+
+# ---- complex64 against the FP64 oracle ----------------------------------------
+
+@pytest.mark.parametrize("n,seed", [(12, 0), (16, 1), (18, 2)])
+def test_c64_random_circuit(n, seed):
+    basis, g = W.random_circuit(n, seed, 200)
+    full = W.basis_gates(n, basis)
+    full.extend(g)
+    with capi.State(n, capi.C64) as s, oracle_state(n, full) as o:
+        s.run(full)
+        a, b = s.amplitudes(), o.amplitudes()
+        assert np.max(np.abs(a - b)) < C64_ATOL
+        assert infidelity(a, b) < C64_INFID
+
+
+def test_c64_brick_circuit_24q():
+    """The brick workload at 24 qubits (the size its oracle runs at)."""
+    n = 24
+    g = W.brick_circuit(n, 6, 7)
+    with capi.State(n, capi.C64) as s, oracle_state(n, g) as o:
+        s.run(g)
+        a, b = s.amplitudes(), o.amplitudes()
+        assert np.max(np.abs(a - b)) < C64_ATOL
+        assert infidelity(a, b) < C64_INFID
+
+
+# ---- reductions and read-out ------------------------------------------------------
+
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_reductions(prec):
+    n = 15
+    _, g = W.random_circuit(n, 5, 120)
+    with capi.State(n, prec) as s, oracle_state(n, g) as o:
+        s.run(g)
+        tol = 1e-6 if prec == capi.C64 else 1e-12
+        assert abs(s.norm_sq() - o.norm_sq()) < tol
+        for q in (0, 3, n - 1):
+            assert abs(s.prob_zero(q) - o.prob_zero(q)) < tol
+            assert abs(s.expect_z(q) - o.expect_z(q)) < 2 * tol
+        for i in (0, 1, 12345, (1 << n) - 1):
+            assert abs(s.probability(i) - o.probability(i)) < tol
+        assert s.probability(1 << n) == 0.0
+        assert s.probability(-1) == 0.0
+
+
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_argmax_exact(prec):
+    for n, idx in ((3, 5), (12, 3000), (20, 777777), (22, (1 << 22) - 1)):
+        with capi.State(n, prec) as s:
+            s.set_basis(idx)
+            assert s.argmax() == idx
+    with capi.State(10, prec) as s:
+        s.set_amplitudes(np.zeros(1 << 10))
+        assert s.argmax() == 0  # all-zero state: index 0 like the reference
+        v = np.zeros(1 << 10, complex)
+        v[[17, 300, 900]] = 0.5  # ties: first index wins
+        s.set_amplitudes(v)
+        assert s.argmax() == 17
+
+
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_measure_with_reference_draws(golden, prec):
+    d = golden("ref_measure_n5")
+    with capi.State(5, prec, capi.REFERENCE) as s:
+        s.run(gates_from(d))
+        outs = [s.measure(int(q), float(r)) for q, r in zip(d["qubits"], d["draws"])]
+        assert outs == list(d["outcomes"])
+        tol = 1e-14 if prec == capi.C128 else 1e-6
+        np.testing.assert_allclose(s.amplitudes(), d["ref"], atol=tol)
+
+
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_measure_collapse_and_normalize(prec):
+    n = 14
+    _, g = W.random_circuit(n, 8, 100, with_qft=False)
+    rng = np.random.default_rng(0)
+    with capi.State(n, prec) as s, oracle_state(n, g) as o:
+        s.run(g)
+        for q in (0, 7, 13, 2):
+            r = float(rng.random())
+            assert s.measure(q, r) == o.measure(q, r)
+        tol = 1e-6 if prec == capi.C64 else 1e-13
+        np.testing.assert_allclose(s.amplitudes(), o.amplitudes(), atol=tol)
+        assert abs(s.norm_sq() - 1.0) < tol
+
+
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_shots_histogram_vs_reference(golden, prec):
+    d = golden("ref_shots_n5")
+    with capi.State(5, prec) as s:
+        s.run(gates_from(d))
+        idx = s.sample(d["draws"])
+    hist = np.bincount(idx[idx >= 0], minlength=32)
+    assert np.array_equal(hist, d["hist"])
+
+
+@pytest.mark.parametrize("n", [10, 13, 17])
+def test_sample_indices_vs_oracle(n):
+    _, g = W.random_circuit(n, 21, 80, with_qft=False)
+    draws = np.random.default_rng(n).random(3000)
+    draws[:3] = [0.0, 1.0, 0.999999999]
+    with capi.State(n, capi.C128) as s, oracle_state(n, g) as o:
+        s.run(g)
+        a = s.sample(draws)
+        b = o.sample(draws)
+        # identical except on a knife edge of FP64 rounding (none expected)
+        assert np.mean(a == b) > 0.999
+        assert a[1] == b[1] == -1 or a[1] == b[1]
+
+
+def test_normalize_rule():
+    with capi.State(6, capi.C128) as s:
+        v = np.zeros(64, complex)
+        v[3] = 2.0
+        v[5] = 1j
+        s.set_amplitudes(v)
+        s.normalize()
+        np.testing.assert_allclose(s.amplitudes(), v / np.sqrt(5.0), atol=1e-15)
+        s.set_amplitudes(np.zeros(64))
+        s.normalize()  # below 1e-12: left alone
+        assert np.all(s.amplitudes() == 0)
+
+
+# ---- Grover -------------------------------------------------------------------------
+
+def test_grover_reference_semantics(golden):
+    d = golden("ref_grover_n6")
+    with capi.State(6, capi.C128, capi.REFERENCE) as s:
+        s.run(gates_from(d))
+        np.testing.assert_allclose(s.amplitudes(), d["ref"], rtol=1e-13, atol=1e-13)
+        assert abs(s.probability(42) - 17.015625) < 1e-9
+
+
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_grover_physical(prec, golden):
+    d = golden("ref_grover_n6")
+    with capi.State(6, prec) as s:
+        s.run(gates_from(d))
+        np.testing.assert_allclose(s.amplitudes(), d["physical"], atol=1e-6)
+        assert s.argmax() == 42
+    n = 12
+    basis, marked, g = W.grover_workload(n, 4, iterations=20)
+    full = W.basis_gates(n, basis)
+    full.extend(g)
+    with capi.State(n, prec) as s, oracle_state(n, full) as o:
+        s.run(full)
+        assert s.argmax() == o.argmax()
+        assert abs(s.probability(marked) - o.probability(marked)) < 1e-5
+
+
+# ---- fused blocks ---------------------------------------------------------------------
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("prec", [capi.C64, capi.C128])
+def test_apply_block_random_unitary(k, prec):
+    n = 11
+    rng = np.random.default_rng(k)
+    for trial in range(3):
+        qubits = list(rng.choice(n, size=k, replace=False))
+        m = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+        u, _ = np.linalg.qr(m)
+        init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        init /= np.linalg.norm(init)
+        with capi.State(n, prec) as s, O.OracleState(n) as o:
+            s.set_amplitudes(init)
+            o.set_amplitudes(init)
+            s.apply_block(qubits, u, capi.FUSE_SIMT)
+            o.apply_block(qubits, u)
+            tol = 1e-5 if prec == capi.C64 else 1e-13
+            np.testing.assert_allclose(s.amplitudes(), o.amplitudes(), atol=tol)
+
+
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
+def test_fused_circuit_simt(k):
+    n = 16
+    g = W.brick_circuit(n, 8, 3)
+    _, r = W.random_circuit(n, 9, 150)
+    g.extend(r)
+    with capi.State(n, capi.C64) as s, oracle_state(n, g) as o:
+        s.run(g, fusion_k=k, engine=capi.FUSE_SIMT)
+        a, b = s.amplitudes(), o.amplitudes()
+        assert np.max(np.abs(a - b)) < C64_ATOL
+        assert infidelity(a, b) < C64_INFID
+    with capi.State(n, capi.C128) as s, oracle_state(n, g) as o:
+        s.run(g, fusion_k=k, engine=capi.FUSE_SIMT)
+        np.testing.assert_allclose(s.amplitudes(), o.amplitudes(), atol=1e-12)
+
+
+def test_fused_with_grover_barriers():
+    n = 11
+    basis, marked, g = W.grover_workload(n, 6, iterations=8)
+    full = W.basis_gates(n, basis)
+    full.extend(g)
+    with capi.State(n, capi.C64) as s, oracle_state(n, full) as o:
+        s.run(full, fusion_k=4)
+        assert s.argmax() == o.argmax()
+        assert infidelity(s.amplitudes(), o.amplitudes()) < C64_INFID
+
+
+# ---- full size: size-independent properties ------------------------------------------
+
+def _inverse(g: W.GateList) -> W.GateList:
+    inv = W.GateList()
+    for k, t, c, a in reversed(list(zip(g.kinds, g.targets, g.controls, g.angles))):
+        if k in (W.RX, W.RY, W.RZ, W.P, W.CPHASE):
+            a = -a
+        elif k not in (W.H, W.X, W.Y, W.Z, W.CNOT):
+            raise ValueError(k)
+        inv.add(k, t, c, a)
+    return inv
+
+
+@pytest.mark.parametrize("fusion_k", [0, 4])
+def test_30q_brick_then_inverse_returns_to_zero(fusion_k):
+    n = 30
+    g = W.brick_circuit(n, 3, 5)
+    with capi.State(n, capi.C64) as s:
+        s.run(g, fusion_k=fusion_k)
+        assert abs(s.norm_sq() - 1.0) < 1e-5
+        s.run(_inverse(g), fusion_k=fusion_k)
+        assert s.argmax() == 0
+        assert s.probability(0) > 1 - 1e-5
+
+
+def test_30q_basis_state_argmax_and_collapse():
+    n = 30
+    idx = (1 << 29) + 123456789
+    with capi.State(n, capi.C64) as s:
+        s.run(W.basis_gates(n, idx))
+        assert s.argmax() == idx
+        s.apply_gate(W.H, 29)
+        assert abs(s.prob_zero(29) - 0.5) < 1e-6
+        assert s.measure(29, 0.25) == 0
+        assert s.argmax() == idx - (1 << 29)
+        assert abs(s.norm_sq() - 1.0) < 1e-6
+
+
+def test_30q_grover_matches_closed_form():
+    """From the uniform state, k iterations give sin^2((2k+1) asin(2^-n/2))."""
+    n = 30
+    marked = 987654321
+    g = W.GateList()
+    for q in range(n):
+        g.add(W.H, q)
+    for _ in range(5):
+        g.add(W.PHASE_FLIP, index=marked)
+        g.add(W.DIFFUSION)
+    with capi.State(n, capi.C64) as s:
+        s.run(g)
+        theta = np.arcsin(2.0 ** (-n / 2))
+        want = np.sin(11 * theta) ** 2
+        assert abs(s.probability(marked) - want) / want < 1e-4
+        assert s.argmax() == marked
+
+
+# ---- error handling -----------------------------------------------------------------------
+
+def test_invalid_arguments():
+    with capi.State(4) as s:
+        for bad in (lambda: s.apply_gate(W.H, 4), lambda: s.apply_gate(W.CNOT, 1, 1),
+                    lambda: s.apply_gate(99, 0), lambda: s.phase_flip(16),
+                    lambda: s.set_basis(-1), lambda: s.apply_block([0, 0], np.eye(4))):
+            with pytest.raises(capi.QcsCudaError) as e:
+                bad()
+            assert e.value.status == capi.EINVAL
+        s.apply_gate(W.X, 0)  # still usable
+        assert s.argmax() == 1
+
+
+def test_injected_failures_leave_library_usable():
+    L = capi.lib()
+    L.qcs_cuda_debug_inject(1, 1)
+    with pytest.raises(capi.QcsCudaError) as e:
+        capi.State(5)
+    assert e.value.status == capi.ENOMEM
+    with capi.State(5) as s:
+        L.qcs_cuda_debug_inject(2, 1)
+        with pytest.raises(capi.QcsCudaError) as e:
+            s.apply_gate(W.H, 0)
+        assert e.value.status == capi.ELAUNCH
+        s.apply_gate(W.X, 2)
+        assert s.argmax() in (4, 5)
+    L.qcs_cuda_debug_inject(0, 0)
