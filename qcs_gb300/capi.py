@@ -369,4 +369,5 @@ def libc() -> C.CDLL:
     L = C.CDLL(None)
     L.rand.restype = C.c_int
     L.srand.argtypes = [C.c_uint]
+    L.fflush.argtypes = [C.c_void_p]
     return L

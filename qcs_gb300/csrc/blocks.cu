@@ -177,15 +177,19 @@ static int apply_block_simt_t(qcs_cuda_state *s, int k, const int *qubits, const
   }
 }
 
-int apply_block(qcs_cuda_state *s, int k, const int *qubits, const double *u, int engine) {
+// Engine choice: the tensor cores take the blocks they support (k = 5, 6 on
+// complex64 states) unless SIMT is asked for; AUTO leaves k <= 4 to the CUDA
+// cores, where the block is bandwidth-bound anyway.  `strict` (explicit
+// single-block calls) refuses a TENSOR request the tensor engine cannot
+// serve instead of running it on the CUDA cores.
+int apply_block(qcs_cuda_state *s, int k, const int *qubits, const double *u, int engine,
+                bool strict) {
   invalidate_sum(s);
-  bool want_tc = engine == QCS_FUSE_TENSOR ||
-                 (engine == QCS_FUSE_AUTO && k > 4 && tc_supported(s, k));
-  if (want_tc) {
-    if (!tc_supported(s, k))
-      return set_error(QCS_CUDA_EUNSUP, "tensor-core block engine: unsupported k=%d / precision", k);
+  const bool tc_ok = tc_supported(s, k);
+  if (engine == QCS_FUSE_TENSOR && strict && !tc_ok)
+    return set_error(QCS_CUDA_EUNSUP, "tensor-core block engine: unsupported k=%d / precision", k);
+  if (tc_ok && (engine == QCS_FUSE_TENSOR || (engine == QCS_FUSE_AUTO && k > 4)))
     return apply_block_tc(s, k, qubits, u);
-  }
   if (s->prec == QCS_CUDA_C128) return apply_block_simt_t<double2>(s, k, qubits, u);
   return apply_block_simt_t<float2>(s, k, qubits, u);
 }
@@ -229,9 +233,8 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
     }
     return QCS_CUDA_OK;
   }
-  if (k > 7) k = 7;
   int engine = opt->fusion_engine;
-  int kcap = engine == QCS_FUSE_SIMT ? kSimtMaxK : 7;
+  int kcap = (engine != QCS_FUSE_SIMT && tc_supported(s, 6)) ? 6 : kSimtMaxK;
   if (k > kcap) k = kcap;
   if (k > s->n) k = s->n;
   PartitionOptions po;
@@ -253,7 +256,8 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
                        u[2].real(), u[2].imag(), u[3].real(), u[3].imag()};
         rc = apply_1q(s, m, it.qubits[0]);
       } else {
-        rc = apply_block(s, kb, it.qubits.data(), reinterpret_cast<const double *>(u.data()), engine);
+        rc = apply_block(s, kb, it.qubits.data(), reinterpret_cast<const double *>(u.data()), engine,
+                         false);
       }
     }
     if (rc) return rc;
@@ -281,7 +285,7 @@ int qcs_cuda_apply_block(qcs_cuda_state *s, int k, const int *qubits, const doub
     if (seen & (1LL << qubits[j])) return set_error(QCS_CUDA_EINVAL, "repeated qubit %d", qubits[j]);
     seen |= 1LL << qubits[j];
   }
-  return apply_block(s, k, qubits, u, engine);
+  return apply_block(s, k, qubits, u, engine, true);
 }
 
 int qcs_cuda_plan(const qcs_cuda_op *ops, int count, int num_qubits, int kmax, int *order,

@@ -1,13 +1,519 @@
-// blocks_tc.cu -- tensor-core (tcgen05) block engine.  Placeholder until the
-// split-BF16x3 kernel lands: reports no support, so AUTO uses the SIMT engine.
+// blocks_tc.cu -- tensor-core (tcgen05) engine for dense k-qubit blocks.
+//
+// The block acts on every column of the state (one setting of the n-k other
+// qubits) as a complex 2^k x 2^k matrix.  Written as a real GEMM,
+//   D[m][o] = sum_i A[m][i] * B[o][i],
+// A = a tile of 128 state columns, row m holding the 2^k amplitudes of
+// column m as interleaved (re, im) reals (i = 2a + c), and B the real form of
+// the block matrix: B[2a'+c'][2a+c] = [[Re U, -Im U], [Im U, Re U]][c'][c]
+// of U[a'][a].  One tile is an M=128 (columns) x N=2^(k+1) (outputs) x
+// K=2^(k+1) (inputs) product on the 5th-generation tensor cores.
+//
+// Precision: split BF16 x 3.  Every FP32 value x is held as hi = bf16(x),
+// lo = bf16(x - hi); D = Ahi*Bhi + Ahi*Blo + Alo*Bhi, accumulated in FP32 in
+// tensor memory.  Relative error per product ~2^-16; over a circuit the
+// infidelity stays far below 1e-6 (checked against the FP64 oracle).
+//
+// Kernel structure (persistent, one CTA per SM, 416 threads):
+//   warps 0-3   epilogue: tcgen05.ld the accumulator (warp w owns TMEM lanes
+//               32w..32w+31 = tile columns), store FP32 results to HBM;
+//   warps 4-11  producers: load the tile's amplitudes from HBM, split into
+//               bf16 hi/lo, write the 128-byte-swizzled K-major operand tile;
+//   warp 12     TMEM allocation and MMA issue (one thread).
+// Operand tiles and TMEM accumulators are double buffered; stages hand over
+// through mbarriers.  Every wait is bounded: on expiry the kernel raises a
+// device error flag, all roles leave their loops, outstanding MMAs are
+// drained and TMEM is freed before exit.
+//
+// Shared memory (k = 6): 2 stages x (hi + lo) x 32 KB state tiles + 64 KB
+// block matrix (hi + lo) + tables ~= 195 KB.  HBM traffic: one read and one
+// write of the state per block, the same as the SIMT engine; tensor work per
+// amplitude 3 x 8 x 2^k flops.
+#include <cuda_bf16.h>
+#include <string.h>
+
+#include <vector>
+
 #include "common.cuh"
 
 namespace qcs {
 
-bool tc_supported(const qcs_cuda_state *, int) { return false; }
+constexpr int kTcM = 128;  // state columns per tile = UMMA M = TMEM lanes
+constexpr int kTcEpiWarps = 4;
+constexpr int kTcProdWarps = 8;
+constexpr int kTcMmaWarp = kTcEpiWarps + kTcProdWarps;  // 12
+constexpr int kTcThreads = (kTcMmaWarp + 1) * 32;        // 416
+constexpr int kTcProdThreads = kTcProdWarps * 32;        // 256
+constexpr int kTcEpiThreads = kTcEpiWarps * 32;          // 128
+constexpr long long kWaitCycles = 4000000000LL;          // ~2 s at 2 GHz
+constexpr int kImgSlots = 8;                             // block-matrix upload ring
 
-int apply_block_tc(qcs_cuda_state *, int, const int *, const double *) {
-  return set_error(QCS_CUDA_EUNSUP, "tensor-core block engine not built");
+template <int KA>  // amplitudes per column (2^k)
+struct TcShape {
+  static constexpr int KD = 2 * KA;              // reals per column: UMMA K extent
+  static constexpr int N = 2 * KA;               // reals out per column: UMMA N
+  static constexpr int A_BYTES = kTcM * KD * 2;  // one bf16 state operand (hi or lo)
+  static constexpr int B_BYTES = N * KD * 2;     // one bf16 matrix operand (hi or lo)
+  static constexpr int KSTEPS = KD / 16;         // UMMA K = 16 for bf16
+  static constexpr int UNITS = kTcM * KA / 4;    // 4-amplitude units per tile
+  static constexpr int UPT = UNITS / kTcProdThreads;
+  static constexpr int TMEM_COLS = 2 * N;        // two accumulator stages
+  static constexpr int OFF_A = 0;                // [stage][hi,lo][A_BYTES]
+  static constexpr int OFF_B = 4 * A_BYTES;      // [hi,lo][B_BYTES]
+  static constexpr int OFF_COL = OFF_B + 2 * B_BYTES;
+  static constexpr int OFF_BLK = OFF_COL + kTcM * 8;
+  static constexpr int OFF_BAR = OFF_BLK + KA * 8;
+  static constexpr int OFF_MISC = OFF_BAR + 8 * 8;
+  static constexpr int SMEM = OFF_MISC + 16 + 1024;  // + slack to align the base to 1 KB
+  static constexpr int IMG_BYTES = 2 * B_BYTES;
+  static_assert(UNITS % kTcProdThreads == 0, "tile units must split over producers");
+  static_assert(KD % 64 == 0, "K extent must be whole 128-byte swizzle atoms");
+  static_assert(TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation size");
+};
+
+struct TcGeom {
+  i64 n_tiles;
+  int nfree;
+  signed char freeq[40];
+  i64 col_off[kTcM];  // column m -> offset (bits of m on the column qubits)
+  i64 blk_off[64];    // block index a -> offset (bit j of a on qubits[j])
+};
+
+// Byte offset of bf16 element (r, k) in a K-major operand of R rows laid out
+// in 128-byte swizzle atoms (8 rows x 64 elements, 16-byte chunks permuted by
+// XOR with the row), atoms along K R*128 bytes apart.
+__host__ __device__ __forceinline__ int sw128_offset(int r, int k, int R) {
+  const int kb = k >> 6, chunk = (k >> 3) & 7, e = k & 7;
+  return kb * (R * 128) + (r >> 3) * 1024 + (r & 7) * 128 + ((chunk ^ (r & 7)) << 4) + e * 2;
+}
+
+// ---- PTX wrappers ---------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ uint32_t mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok;
+}
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+// D (TMEM) [+]= A (smem desc) * B (smem desc)^T, bf16 in, fp32 accumulate.
+__device__ __forceinline__ void umma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// Arrive on `bar` once every MMA issued so far by this thread has completed.
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+// 32 consecutive TMEM columns of this warp's 32 lanes; waits for completion
+// inside the same statement so the registers are never read early.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *out) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) out[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO); the leading offset is unused for this layout.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;             // LBO (ignored for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // SBO
+  d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = bf16, D = fp32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+// Bounded mbarrier wait.  Returns false when the CTA is aborting.
+__device__ __noinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                      int *err, int where) {
+  long long t0 = clock64();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      *abort_flag = 1;
+      atomicExch(err, where);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
+  i64 b = 0;
+  for (int j = 0; j < g.nfree; j++) b |= ((tile >> j) & 1LL) << g.freeq[j];
+  return b;
+}
+
+template <int KA, bool COL_FAST>
+__device__ __forceinline__ void unit_coords(int u, int &m, int &j) {
+  if (COL_FAST) {  // consecutive threads walk consecutive columns (qubit 0 is a column bit)
+    m = u & (kTcM - 1);
+    j = u >> 7;
+  } else {         // consecutive threads walk a column's amplitudes (qubit 0 in the block)
+    j = u & (KA / 4 - 1);
+    m = u / (KA / 4);
+  }
+}
+
+template <int KA, bool COL_FAST>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_block_tc(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int *err) {
+  using S = TcShape<KA>;
+  extern __shared__ uint8_t smem_dyn[];
+  const uint32_t raw = smem_u32(smem_dyn);
+  uint8_t *smem = smem_dyn + ((1024u - (raw & 1023u)) & 1023u);
+  uint8_t *sA = smem + S::OFF_A;
+  uint8_t *sB = smem + S::OFF_B;
+  i64 *col_off = reinterpret_cast<i64 *>(smem + S::OFF_COL);
+  i64 *blk_off = reinterpret_cast<i64 *>(smem + S::OFF_BLK);
+  const uint32_t bar0 = smem_u32(smem + S::OFF_BAR);  // 8-byte barriers:
+  // 0,1 a_full[stage]  2,3 mma_done[stage]  4,5 acc_empty[stage]  6 drain
+  auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::OFF_MISC);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::OFF_MISC + 4);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    mbar_init(bar(0), kTcProdThreads);
+    mbar_init(bar(1), kTcProdThreads);
+    mbar_init(bar(2), 1);
+    mbar_init(bar(3), 1);
+    mbar_init(bar(4), kTcEpiThreads);
+    mbar_init(bar(5), kTcEpiThreads);
+    mbar_init(bar(6), 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  for (int i = tid; i < kTcM; i += kTcThreads) col_off[i] = g.col_off[i];
+  for (int i = tid; i < KA; i += kTcThreads) blk_off[i] = g.blk_off[i];
+  {
+    uint4 *dst = reinterpret_cast<uint4 *>(sB);
+    for (int i = tid; i < S::IMG_BYTES / 16; i += kTcThreads) dst[i] = bimg[i];
+  }
+  fence_async_shared();  // the block matrix is read by the tensor cores
+  if (warp == kTcMmaWarp) {
+    tmem_alloc(smem_u32(tmem_slot), S::TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp >= kTcEpiWarps && warp < kTcMmaWarp) {
+    // ---------------- producers ----------------
+    const int p = tid - kTcEpiThreads;
+    int it = 0;
+    for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
+      const int stage = it & 1;
+      if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
+      const i64 base = tile_base(tile, g);
+      float2 x[S::UPT][4];
+#pragma unroll
+      for (int i = 0; i < S::UPT; i++) {
+        int m, j;
+        unit_coords<KA, COL_FAST>(p + i * kTcProdThreads, m, j);
+        const float2 *src = v + base + col_off[m];
+#pragma unroll
+        for (int e = 0; e < 4; e++) x[i][e] = src[blk_off[4 * j + e]];
+      }
+      uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
+      uint8_t *alo = ahi + S::A_BYTES;
+#pragma unroll
+      for (int i = 0; i < S::UPT; i++) {
+        int m, j;
+        unit_coords<KA, COL_FAST>(p + i * kTcProdThreads, m, j);
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          __nv_bfloat162 hb = __floats2bfloat162_rn(x[i][e].x, x[i][e].y);
+          float2 hf = __bfloat1622float2(hb);
+          __nv_bfloat162 lb = __floats2bfloat162_rn(x[i][e].x - hf.x, x[i][e].y - hf.y);
+          h[e] = *reinterpret_cast<uint32_t *>(&hb);
+          l[e] = *reinterpret_cast<uint32_t *>(&lb);
+        }
+        const int off = sw128_offset(m, 8 * j, kTcM);
+        *reinterpret_cast<uint4 *>(ahi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(alo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+      }
+      fence_async_shared();
+      mbar_arrive(bar(stage));
+    }
+  } else if (warp == kTcMmaWarp) {
+    // ---------------- MMA issue ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(kTcM, S::N);
+      const uint32_t a0 = smem_u32(sA), b_hi = smem_u32(sB), b_lo = b_hi + S::B_BYTES;
+      int it = 0;
+      for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
+        const int stage = it & 1;
+        if (!wait_bar(bar(stage), (it >> 1) & 1, abort_flag, err, 2)) break;
+        if (it >= 2 && !wait_bar(bar(4 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 3)) break;
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(stage * S::N);
+        const uint32_t a_hi = a0 + (uint32_t)(2 * stage * S::A_BYTES);
+        const uint32_t a_lo = a_hi + S::A_BYTES;
+#pragma unroll
+        for (int s = 0; s < S::KSTEPS; s++) {
+          const uint32_t ka = (uint32_t)((s >> 2) * (kTcM * 128) + (s & 3) * 32);
+          const uint32_t kb = (uint32_t)((s >> 2) * (S::N * 128) + (s & 3) * 32);
+          umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_hi + kb), idesc, s > 0 ? 1u : 0u);
+          umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_lo + kb), idesc, 1u);
+          umma_bf16(d, sw128_desc(a_lo + ka), sw128_desc(b_hi + kb), idesc, 1u);
+        }
+        umma_commit(bar(2 + stage));
+      }
+      // every MMA issued above must finish before TMEM is released
+      umma_commit(bar(6));
+      long long t0 = clock64();
+      while (!mbar_try_wait(bar(6), 0)) {
+        if (clock64() - t0 > kWaitCycles) {
+          atomicExch(err, 4);
+          break;
+        }
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- epilogue ----------------
+    const int m = tid;  // TMEM lane = tile column
+    const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
+    int it = 0;
+    for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
+      const int stage = it & 1;
+      if (!wait_bar(bar(2 + stage), (it >> 1) & 1, abort_flag, err, 5)) break;
+      tc_fence_after();
+      float2 *dst = v + tile_base(tile, g) + col_off[m];
+#pragma unroll 1
+      for (int c = 0; c < S::N / 32; c++) {
+        float acc[32];
+        tmem_ld32(tmem + lane_addr + (uint32_t)(stage * S::N + 32 * c), acc);
+#pragma unroll
+        for (int q = 0; q < 16; q++) dst[blk_off[16 * c + q]] = make_float2(acc[2 * q], acc[2 * q + 1]);
+      }
+      tc_fence_before();
+      mbar_arrive(bar(4 + stage));
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kTcMmaWarp) {
+    tc_fence_after();
+    tmem_dealloc(tmem, S::TMEM_COLS);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+struct TcRing {
+  uint8_t *host = nullptr;  // pinned, kImgSlots images
+  uint8_t *dev = nullptr;
+  cudaEvent_t done[kImgSlots] = {};
+  int next = 0;
+  int *d_err = nullptr;
+};
+
+static uint16_t bf16_rn(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+static float bf16_to_float(uint16_t h) {
+  uint32_t u = (uint32_t)h << 16;
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+
+// Block matrix u (K x K complex, row-major) -> swizzled hi/lo image of B.
+template <int KA>
+static void make_image(const double *u, uint8_t *img) {
+  using S = TcShape<KA>;
+  memset(img, 0, S::IMG_BYTES);
+  uint16_t *hi = reinterpret_cast<uint16_t *>(img);
+  uint16_t *lo = reinterpret_cast<uint16_t *>(img + S::B_BYTES);
+  for (int ao = 0; ao < KA; ao++)
+    for (int ai = 0; ai < KA; ai++) {
+      const double re = u[2 * (ao * KA + ai)], im = u[2 * (ao * KA + ai) + 1];
+      const double blk[2][2] = {{re, -im}, {im, re}};
+      for (int co = 0; co < 2; co++)
+        for (int ci = 0; ci < 2; ci++) {
+          const int o = 2 * ao + co, i = 2 * ai + ci;
+          const double x = blk[co][ci];
+          const uint16_t h = bf16_rn((float)x);
+          const uint16_t l = bf16_rn((float)(x - (double)bf16_to_float(h)));
+          const int off = sw128_offset(o, i, S::N) / 2;
+          hi[off] = h;
+          lo[off] = l;
+        }
+    }
+}
+
+static int ring_init(qcs_cuda_state *s) {
+  if (s->tc) return QCS_CUDA_OK;
+  TcRing *r = new TcRing();
+  const size_t bytes = (size_t)kImgSlots * TcShape<64>::IMG_BYTES;
+  int rc = check_cuda(cudaMallocHost((void **)&r->host, bytes), "cudaMallocHost(block images)");
+  if (!rc) rc = check_cuda(cudaMalloc((void **)&r->dev, bytes), "cudaMalloc(block images)");
+  for (int i = 0; !rc && i < kImgSlots; i++)
+    rc = check_cuda(cudaEventCreateWithFlags(&r->done[i], cudaEventDisableTiming), "cudaEventCreate");
+  if (rc) {
+    tc_release(r);
+    return rc;
+  }
+  s->tc = r;
+  return QCS_CUDA_OK;
+}
+
+void tc_release(TcRing *r) {
+  if (!r) return;
+  for (int i = 0; i < kImgSlots; i++)
+    if (r->done[i]) cudaEventDestroy(r->done[i]);
+  if (r->host) cudaFreeHost(r->host);
+  if (r->dev) cudaFree(r->dev);
+  delete r;
+}
+
+bool tc_supported(const qcs_cuda_state *s, int k) {
+  return s->prec == QCS_CUDA_C64 && s->sem == QCS_CUDA_PHYSICAL && (k == 5 || k == 6) &&
+         s->n >= k + 7 && s->n - k - 7 <= 40 && s->dev.cc_major == 10 && s->dev.cc_minor == 3;
+}
+
+template <int KA, bool COL_FAST>
+static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img) {
+  using S = TcShape<KA>;
+  static bool configured = false;
+  if (!configured) {
+    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc<KA, COL_FAST>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM),
+                        "cudaFuncSetAttribute(tcgen05 block)");
+    if (rc) return rc;
+    configured = true;
+  }
+  const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
+  prof_begin(s);
+  k_block_tc<KA, COL_FAST><<<grid, kTcThreads, S::SMEM, s->stream>>>(
+      (float2 *)s->vec, g, img, s->d_err);
+  return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
+}
+
+int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u) {
+  int rc = ring_init(s);
+  if (rc) return rc;
+  TcRing *r = s->tc;
+  // geometry
+  TcGeom g;
+  memset(&g, 0, sizeof(g));
+  std::vector<int> role(s->n, -1);  // >= 0 block bit, -2 column, -1 free
+  for (int j = 0; j < k; j++) role[qubits[j]] = j;
+  std::vector<int> colq;
+  for (int q = 0; q < s->n && (int)colq.size() < 7; q++)
+    if (role[q] == -1) {
+      role[q] = -2;
+      colq.push_back(q);
+    }
+  for (int q = 0; q < s->n; q++)
+    if (role[q] == -1) g.freeq[g.nfree++] = (signed char)q;
+  g.n_tiles = 1LL << g.nfree;
+  for (int m = 0; m < kTcM; m++) {
+    i64 o = 0;
+    for (int b = 0; b < 7; b++)
+      if ((m >> b) & 1) o |= 1LL << colq[b];
+    g.col_off[m] = o;
+  }
+  const int KA = 1 << k;
+  for (int a = 0; a < KA; a++) {
+    i64 o = 0;
+    for (int j = 0; j < k; j++)
+      if ((a >> j) & 1) o |= 1LL << qubits[j];
+    g.blk_off[a] = o;
+  }
+  const bool col_fast = role[0] == -2;
+  // block-matrix image through the pinned ring
+  const int slot = r->next;
+  r->next = (r->next + 1) % kImgSlots;
+  rc = check_cuda(cudaEventSynchronize(r->done[slot]), "block image slot");
+  if (rc) return rc;
+  const size_t img_bytes = (size_t)TcShape<64>::IMG_BYTES;
+  uint8_t *h = r->host + slot * img_bytes;
+  uint8_t *d = r->dev + slot * img_bytes;
+  if (k == 6) make_image<64>(u, h);
+  else make_image<32>(u, h);
+  const size_t used = k == 6 ? TcShape<64>::IMG_BYTES : TcShape<32>::IMG_BYTES;
+  rc = check_cuda(cudaMemcpyAsync(d, h, used, cudaMemcpyHostToDevice, s->stream),
+                  "block image upload");
+  if (rc) return rc;
+  const uint4 *img = reinterpret_cast<const uint4 *>(d);
+  if (k == 6) rc = col_fast ? launch_tc<64, true>(s, g, img) : launch_tc<64, false>(s, g, img);
+  else rc = col_fast ? launch_tc<32, true>(s, g, img) : launch_tc<32, false>(s, g, img);
+  if (rc) return rc;
+  return check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
 }
 
 }  // namespace qcs

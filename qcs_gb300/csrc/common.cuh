@@ -50,6 +50,8 @@ enum KClass {
 };
 
 struct ProfData;  // per-state event bookkeeping (state.cu)
+struct TcRing;    // tensor-core engine block-matrix uploads (blocks_tc.cu)
+void tc_release(TcRing *r);
 
 }  // namespace qcs
 
@@ -80,6 +82,8 @@ struct qcs_cuda_state {
   // measurement support
   long long launches;
   qcs::ProfData *prof;    // non-null while profiling
+  qcs::TcRing *tc;        // created on first tensor-core block
+  int *d_err;             // device error flag (bounded waits that gave up)
 };
 
 namespace qcs {

@@ -188,6 +188,8 @@ static void free_state(qcs_cuda_state *s) {
   if (!s) return;
   if (s->stream) cudaStreamSynchronize(s->stream);
   prof_free(s);
+  tc_release(s->tc);
+  cudaFree(s->d_err);
   cudaFree(s->vec);
   cudaFree(s->scratch);
   cudaFree(s->d_partials);
@@ -317,6 +319,8 @@ int qcs_cuda_state_create(int num_qubits, int precision, int semantics,
   if (!rc) rc = dmalloc((void **)&s->d_partials,
                         (size_t)s->dev.reduce_blocks * sizeof(ReduceSlot), "cudaMalloc(partials)");
   if (!rc) rc = dmalloc((void **)&s->d_result, 8 * sizeof(double), "cudaMalloc(result)");
+  if (!rc) rc = dmalloc((void **)&s->d_err, sizeof(int), "cudaMalloc(error flag)");
+  if (!rc) rc = check_cuda(cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream), "cudaMemset(err)");
   if (!rc) rc = check_cuda(cudaMallocHost((void **)&s->h_result, 8 * sizeof(double)),
                            "cudaMallocHost(result)");
   if (!rc) rc = check_cuda(cudaMemsetAsync(s->vec, 0, bytes, s->stream), "cudaMemset(state)");
@@ -362,7 +366,16 @@ int qcs_cuda_state_device_ptr(qcs_cuda_state *s, void **ptr) {
 
 int qcs_cuda_synchronize(qcs_cuda_state *s) {
   QCS_CHECK_STATE(s);
-  return check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+  int rc = check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+  if (rc) return rc;
+  int flag = 0;
+  rc = check_cuda(cudaMemcpy(&flag, s->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+  if (rc) return rc;
+  if (flag) {
+    cudaMemset(s->d_err, 0, sizeof(int));
+    return set_error(QCS_CUDA_ETIMEOUT, "a bounded device-side wait gave up (site %d)", flag);
+  }
+  return QCS_CUDA_OK;
 }
 
 int qcs_cuda_set_basis(qcs_cuda_state *s, long long index) {

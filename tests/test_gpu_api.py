@@ -190,6 +190,7 @@ def test_qc_print(A, capfd):
     A.qc_print_state(c, -1)
     A.qc_print_circuit(c)
     A.qc_destroy(c)
+    capi.libc().fflush(None)  # C stdio buffers stdout when it is not a terminal
     out = capfd.readouterr().out
     assert "--- Quantum State (1 Qubits) ---" in out
     assert "|0>: 0.707107 + i0.000000" in out

@@ -286,6 +286,58 @@ def test_fused_circuit_simt(k):
         np.testing.assert_allclose(s.amplitudes(), o.amplitudes(), atol=1e-12)
 
 
+# Tensor-core engine (split BF16 x 3, FP32 accumulation): per-block relative
+# error ~2^-16, so the bars are infidelity <= 1e-8 per block and <= 1e-6 over a
+# circuit, and max |delta| <= 5e-5.
+TC_ATOL = 5e-5
+
+
+@pytest.mark.parametrize("k", [5, 6])
+@pytest.mark.parametrize("with_q0", [False, True])
+def test_apply_block_tensor_cores(k, with_q0):
+    n = 15
+    rng = np.random.default_rng(10 * k + with_q0)
+    for trial in range(3):
+        rest = [q for q in range(1, n)]
+        qubits = list(rng.choice(rest, size=k - 1 if with_q0 else k, replace=False))
+        if with_q0:
+            qubits.insert(int(rng.integers(0, k)), 0)
+        m = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+        u, _ = np.linalg.qr(m)
+        init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        init /= np.linalg.norm(init)
+        with capi.State(n, capi.C64) as s, O.OracleState(n) as o:
+            s.set_amplitudes(init)
+            o.set_amplitudes(init)
+            s.apply_block(qubits, u, capi.FUSE_TENSOR)
+            o.apply_block(qubits, u)
+            s.synchronize()
+            a, b = s.amplitudes(), o.amplitudes()
+            assert np.max(np.abs(a - b)) < TC_ATOL
+            assert infidelity(a, b) < 1e-8
+
+
+def test_tensor_engine_rejects_unsupported():
+    with capi.State(12, capi.C128) as s:
+        with pytest.raises(capi.QcsCudaError) as e:
+            s.apply_block(list(range(6)), np.eye(64), capi.FUSE_TENSOR)
+        assert e.value.status == capi.EUNSUP
+
+
+@pytest.mark.parametrize("k", [5, 6])
+def test_fused_circuit_tensor_cores(k):
+    n = 18
+    g = W.brick_circuit(n, 10, 4)
+    _, r = W.random_circuit(n, 12, 200)
+    g.extend(r)
+    with capi.State(n, capi.C64) as s, oracle_state(n, g) as o:
+        s.run(g, fusion_k=k, engine=capi.FUSE_TENSOR)
+        s.synchronize()
+        a, b = s.amplitudes(), o.amplitudes()
+        assert np.max(np.abs(a - b)) < TC_ATOL
+        assert infidelity(a, b) < 1e-6
+
+
 def test_fused_with_grover_barriers():
     n = 11
     basis, marked, g = W.grover_workload(n, 6, iterations=8)
@@ -310,14 +362,16 @@ def _inverse(g: W.GateList) -> W.GateList:
     return inv
 
 
-@pytest.mark.parametrize("fusion_k", [0, 4])
-def test_30q_brick_then_inverse_returns_to_zero(fusion_k):
+@pytest.mark.parametrize("fusion_k,engine", [(0, capi.FUSE_AUTO), (4, capi.FUSE_SIMT),
+                                             (6, capi.FUSE_TENSOR)])
+def test_30q_brick_then_inverse_returns_to_zero(fusion_k, engine):
     n = 30
     g = W.brick_circuit(n, 3, 5)
     with capi.State(n, capi.C64) as s:
-        s.run(g, fusion_k=fusion_k)
+        s.run(g, fusion_k=fusion_k, engine=engine)
         assert abs(s.norm_sq() - 1.0) < 1e-5
-        s.run(_inverse(g), fusion_k=fusion_k)
+        s.run(_inverse(g), fusion_k=fusion_k, engine=engine)
+        s.synchronize()
         assert s.argmax() == 0
         assert s.probability(0) > 1 - 1e-5
 
