@@ -65,6 +65,7 @@ def lib() -> C.CDLL:
             "orc_apply_controlled": (i, [vp, dp, i, i]),
             "orc_apply_gate": (i, [vp, i, i, i, d]),
             "orc_run_gates": (i, [vp, i, ip, ip, ip, dp]),
+            "orc_run_ops": (i, [vp, i, ip, ip, ip, dp, lp]),
             "orc_apply_block": (i, [vp, i, ip, dp]),
             "orc_phase_flip": (i, [vp, l]),
             "orc_diffusion": (i, [vp]),
@@ -157,7 +158,9 @@ class OracleState:
         t = np.ascontiguousarray(gates.targets, dtype=np.int32)
         c = np.ascontiguousarray(gates.controls, dtype=np.int32)
         a = np.ascontiguousarray(gates.angles, dtype=np.float64)
-        rc = lib().orc_run_gates(self._h, len(k), _ip(k), _ip(t), _ip(c), _dp(a))
+        ix = np.ascontiguousarray(getattr(gates, "indices", [0] * len(k)), dtype=np.int64)
+        rc = lib().orc_run_ops(self._h, len(k), _ip(k), _ip(t), _ip(c), _dp(a),
+                               ix.ctypes.data_as(C.POINTER(C.c_long)))
         if rc != 0:
             raise ValueError("oracle: invalid gate in list")
 

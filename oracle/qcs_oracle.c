@@ -298,6 +298,24 @@ int orc_run_gates(orc_state *s, int count, const int *kinds,
   return 0;
 }
 
+int orc_run_ops(orc_state *s, int count, const int *kinds, const int *targets,
+                const int *controls, const double *angles,
+                const long *indices) {
+  int i;
+  int rc;
+  for (i = 0; i < count; i++) {
+    if (kinds[i] == ORC_OP_PHASE_FLIP)
+      rc = orc_phase_flip(s, indices[i]);
+    else if (kinds[i] == ORC_OP_DIFFUSION)
+      rc = orc_diffusion(s);
+    else
+      rc = orc_apply_gate(s, kinds[i], targets[i], controls[i], angles[i]);
+    if (rc != 0)
+      return rc;
+  }
+  return 0;
+}
+
 /* Dense 2^k x 2^k block on an ordered qubit list (bit j of the block index
  * is qubit qubits[j]); u is row-major (re,im).  The reference has no fused
  * path; its dense N x N apply (src/q_matrix.c:59-96) is the closest

@@ -52,6 +52,8 @@ extern "C" {
 #define ORC_GATE_CNOT 8
 #define ORC_GATE_CPHASE 9
 #define ORC_GATE_I 10
+#define ORC_OP_PHASE_FLIP 20
+#define ORC_OP_DIFFUSION 21
 
 typedef struct orc_state orc_state;
 
@@ -74,6 +76,11 @@ int orc_apply_gate(orc_state *s, int kind, int target, int control,
 int orc_run_gates(orc_state *s, int count, const int *kinds,
                   const int *targets, const int *controls,
                   const double *angles);
+/* As orc_run_gates, plus the non-gate operations ORC_OP_PHASE_FLIP (index)
+ * and ORC_OP_DIFFUSION. */
+int orc_run_ops(orc_state *s, int count, const int *kinds, const int *targets,
+                const int *controls, const double *angles,
+                const long *indices);
 int orc_apply_block(orc_state *s, int k, const int *qubits, const double *u);
 
 int orc_phase_flip(orc_state *s, long index);

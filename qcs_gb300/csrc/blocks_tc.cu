@@ -9,26 +9,31 @@
 // of U[a'][a].  One tile is an M=128 (columns) x N=2^(k+1) (outputs) x
 // K=2^(k+1) (inputs) product on the 5th-generation tensor cores.
 //
-// Precision: split BF16 x 3.  Every FP32 value x is held as hi = bf16(x),
-// lo = bf16(x - hi); D = Ahi*Bhi + Ahi*Blo + Alo*Bhi, accumulated in FP32 in
-// tensor memory.  Relative error per product ~2^-16; over a circuit the
-// infidelity stays far below 1e-6 (checked against the FP64 oracle).
+// Precision: split BF16.  Each state value x is held as hi = bf16(x),
+// lo = bf16(x - hi) (16 significant bits); each block-matrix entry as
+// hi + mid + lo (24 bits).  D = Ahi*Bhi + Ahi*Bmid + Ahi*Blo + Alo*Bhi,
+// accumulated in FP32 in tensor memory.  The state's representation error is
+// random from amplitude to amplitude; the matrix's is the same for every
+// column, so the matrix gets the third term: a 16-bit matrix makes the
+// applied operator non-unitary by ~1e-6 per block, a systematic norm drift
+// that 24 bits removes.
 //
 // Kernel structure (persistent, one CTA per SM, 416 threads):
 //   warps 0-3   epilogue: tcgen05.ld the accumulator (warp w owns TMEM lanes
 //               32w..32w+31 = tile columns), store FP32 results to HBM;
 //   warps 4-11  producers: load the tile's amplitudes from HBM, split into
 //               bf16 hi/lo, write the 128-byte-swizzled K-major operand tile;
+//               (the block matrix stays resident in shared memory)
 //   warp 12     TMEM allocation and MMA issue (one thread).
 // Operand tiles and TMEM accumulators are double buffered; stages hand over
 // through mbarriers.  Every wait is bounded: on expiry the kernel raises a
 // device error flag, all roles leave their loops, outstanding MMAs are
 // drained and TMEM is freed before exit.
 //
-// Shared memory (k = 6): 2 stages x (hi + lo) x 32 KB state tiles + 64 KB
-// block matrix (hi + lo) + tables ~= 195 KB.  HBM traffic: one read and one
-// write of the state per block, the same as the SIMT engine; tensor work per
-// amplitude 3 x 8 x 2^k flops.
+// Shared memory (k = 6): 2 stages x (hi + lo) x 32 KB state tiles + 96 KB
+// block matrix (hi + mid + lo) + tables = 226.6 KB.  HBM traffic: one read
+// and one write of the state per block, the same as the SIMT engine; tensor
+// work per amplitude 4 x 8 x 2^k flops.
 #include <cuda_bf16.h>
 #include <string.h>
 
@@ -59,13 +64,14 @@ struct TcShape {
   static constexpr int UPT = UNITS / kTcProdThreads;
   static constexpr int TMEM_COLS = 2 * N;        // two accumulator stages
   static constexpr int OFF_A = 0;                // [stage][hi,lo][A_BYTES]
-  static constexpr int OFF_B = 4 * A_BYTES;      // [hi,lo][B_BYTES]
-  static constexpr int OFF_COL = OFF_B + 2 * B_BYTES;
+  static constexpr int OFF_B = 4 * A_BYTES;      // [hi,mid,lo][B_BYTES]
+  static constexpr int OFF_COL = OFF_B + 3 * B_BYTES;
   static constexpr int OFF_BLK = OFF_COL + kTcM * 8;
   static constexpr int OFF_BAR = OFF_BLK + KA * 8;
   static constexpr int OFF_MISC = OFF_BAR + 8 * 8;
   static constexpr int SMEM = OFF_MISC + 16 + 1024;  // + slack to align the base to 1 KB
-  static constexpr int IMG_BYTES = 2 * B_BYTES;
+  static constexpr int IMG_BYTES = 3 * B_BYTES;
+  static_assert(SMEM <= 232448, "exceeds the 227 KB shared-memory opt-in");
   static_assert(UNITS % kTcProdThreads == 0, "tile units must split over producers");
   static_assert(KD % 64 == 0, "K extent must be whole 128-byte swizzle atoms");
   static_assert(TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation size");
@@ -304,7 +310,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // ---------------- MMA issue ----------------
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(kTcM, S::N);
-      const uint32_t a0 = smem_u32(sA), b_hi = smem_u32(sB), b_lo = b_hi + S::B_BYTES;
+      const uint32_t a0 = smem_u32(sA), b_hi = smem_u32(sB);
+      const uint32_t b_mid = b_hi + S::B_BYTES, b_lo = b_mid + S::B_BYTES;
       int it = 0;
       for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
         const int stage = it & 1;
@@ -319,6 +326,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const uint32_t ka = (uint32_t)((s >> 2) * (kTcM * 128) + (s & 3) * 32);
           const uint32_t kb = (uint32_t)((s >> 2) * (S::N * 128) + (s & 3) * 32);
           umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_hi + kb), idesc, s > 0 ? 1u : 0u);
+          umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_mid + kb), idesc, 1u);
           umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_lo + kb), idesc, 1u);
           umma_bf16(d, sw128_desc(a_lo + ka), sw128_desc(b_hi + kb), idesc, 1u);
         }
@@ -391,13 +399,14 @@ static float bf16_to_float(uint16_t h) {
   return f;
 }
 
-// Block matrix u (K x K complex, row-major) -> swizzled hi/lo image of B.
+// Block matrix u (K x K complex, row-major) -> swizzled hi/mid/lo image of B.
 template <int KA>
 static void make_image(const double *u, uint8_t *img) {
   using S = TcShape<KA>;
   memset(img, 0, S::IMG_BYTES);
   uint16_t *hi = reinterpret_cast<uint16_t *>(img);
-  uint16_t *lo = reinterpret_cast<uint16_t *>(img + S::B_BYTES);
+  uint16_t *mid = reinterpret_cast<uint16_t *>(img + S::B_BYTES);
+  uint16_t *lo = reinterpret_cast<uint16_t *>(img + 2 * S::B_BYTES);
   for (int ao = 0; ao < KA; ao++)
     for (int ai = 0; ai < KA; ai++) {
       const double re = u[2 * (ao * KA + ai)], im = u[2 * (ao * KA + ai) + 1];
@@ -407,9 +416,12 @@ static void make_image(const double *u, uint8_t *img) {
           const int o = 2 * ao + co, i = 2 * ai + ci;
           const double x = blk[co][ci];
           const uint16_t h = bf16_rn((float)x);
-          const uint16_t l = bf16_rn((float)(x - (double)bf16_to_float(h)));
+          const double r1 = x - (double)bf16_to_float(h);
+          const uint16_t m = bf16_rn((float)r1);
+          const uint16_t l = bf16_rn((float)(r1 - (double)bf16_to_float(m)));
           const int off = sw128_offset(o, i, S::N) / 2;
           hi[off] = h;
+          mid[off] = m;
           lo[off] = l;
         }
     }

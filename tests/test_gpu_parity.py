@@ -203,9 +203,12 @@ def test_sample_indices_vs_oracle(n):
         s.run(g)
         a = s.sample(draws)
         b = o.sample(draws)
-        # identical except on a knife edge of FP64 rounding (none expected)
-        assert np.mean(a == b) > 0.999
-        assert a[1] == b[1] == -1 or a[1] == b[1]
+        # identical except on a knife edge of FP64 rounding: the draw r = 1.0
+        # sits on the total, which the reference's sequential sum and the
+        # device's tree sum round differently (-1 or the last index)
+        assert np.array_equal(a[2:], b[2:])
+        assert a[0] == b[0]
+        assert a[1] in (-1, b[1])
 
 
 def test_normalize_rule():
