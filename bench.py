@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--depth", type=int, default=40)
     ap.add_argument("--seed", type=int, default=2026)
-    ap.add_argument("--fusion-k", type=int, default=int(os.environ.get("QCS_BENCH_FUSION_K", "5")))
+    ap.add_argument("--fusion-k", type=int, default=int(os.environ.get("QCS_BENCH_FUSION_K", "6")))
     ap.add_argument("--engine", default=os.environ.get("QCS_BENCH_ENGINE", "auto"),
                     choices=["auto", "simt", "tensor"])
     ap.add_argument("--plain-steps", type=int, default=None,
@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--parity-qubits", type=int, default=24)
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--cpu-sample-gates", type=int, default=48)
+    ap.add_argument("--sweeps", action="store_true",
+                    help="time each sweep type alone (HBM GB/s per kernel class)")
+    ap.add_argument("--only", default=None,
+                    help="with --sweeps: comma-separated subset of sweep types")
     return ap.parse_args()
 
 
@@ -419,11 +423,82 @@ def run_ours(args, dist):
         print(json.dumps(line), flush=True)
 
 
+SWEEPS = ("dense1q", "diag1q", "phase_mask", "ctrl1q", "cphase", "block_simt4",
+          "block_tc6", "block_tc5", "norm", "argmax", "diffuse", "measure", "sample")
+
+
+def run_sweeps(args, dist):
+    """Each sweep type alone on an n-qubit complex64 state: W untimed and K
+    timed launches bracketed by CUDA events on the state's stream.  Reports
+    device time per launch and algorithmic GB/s against the measured HBM peak.
+    The kernels are timed in isolation, so the burst peak applies."""
+    from qcs_gb300 import build as B
+    from qcs_gb300 import capi
+    from qcs_gb300 import workloads as W
+    B.build()
+    n = args.qubits
+    only = args.only.split(",") if args.only else SWEEPS
+    peak = measured_peaks()
+    rng = np.random.default_rng(args.seed)
+    out = {}
+    with capi.State(n, capi.C64) as s:
+        s.run(W.brick_circuit(n, 1, args.seed))  # a generic dense state (plain kernels)
+        s.synchronize()
+        u6, _ = np.linalg.qr(rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64)))
+        u5, _ = np.linalg.qr(rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32)))
+        u4, _ = np.linalg.qr(rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16)))
+        draws = rng.random(1024)
+        Ns = float(s.size) * 8
+        ops = {
+            "dense1q": (lambda i: s.apply_gate(W.RY, (7 * i) % n, -1, 0.3), 2 * Ns),
+            "diag1q": (lambda i: s.apply_gate(W.RZ, (7 * i) % n, -1, 0.3), 2 * Ns),
+            "phase_mask": (lambda i: s.apply_gate(W.P, (7 * i) % n, -1, 0.3), Ns),
+            "ctrl1q": (lambda i: s.apply_gate(W.CNOT, (7 * i + 3) % n, (7 * i) % n), Ns),
+            "cphase": (lambda i: s.apply_gate(W.CPHASE, (7 * i + 3) % n, (7 * i) % n, 0.3),
+                       Ns / 2),
+            "block_simt4": (lambda i: s.apply_block([(i + 2 * j) % n for j in range(4)], u4,
+                                                    capi.FUSE_SIMT), 2 * Ns),
+            "block_tc6": (lambda i: s.apply_block([(i + 3 * j) % n for j in range(6)], u6,
+                                                  capi.FUSE_TENSOR), 2 * Ns),
+            "block_tc5": (lambda i: s.apply_block([(i + 3 * j) % n for j in range(5)], u5,
+                                                  capi.FUSE_TENSOR), 2 * Ns),
+            "norm": (lambda i: s.norm_sq(), Ns),
+            "argmax": (lambda i: s.argmax(), Ns),
+            "diffuse": (lambda i: s.diffusion(), 2 * Ns),
+            "measure": (lambda i: s.measure(i % n, 0.5), 2.5 * Ns),
+            "sample": (lambda i: s.sample(draws), Ns),
+        }
+        for name in only:
+            fn, nbytes = ops[name]
+            for i in range(args.warmup):
+                fn(i)
+            s.synchronize()
+            s.profile(True)
+            e0 = s.event()
+            for i in range(args.steps):
+                fn(i)
+            e1 = s.event()
+            ms = capi.State.elapsed_ms(e0, e1) / args.steps
+            prof = s.profile_read()
+            s.profile(False)
+            main_cls = max(prof.items(), key=lambda kv: kv[1][1])
+            out[name] = {"ms_per_launch": ms, "GB/s": nbytes / (ms / 1e3) / 1e9,
+                         "frac_of_hbm": nbytes / (ms / 1e3) / 1e9 / peak["hbm_gbs"],
+                         "kernel_class": main_cls[0],
+                         "kernel_ms": main_cls[1][1] / max(1, main_cls[1][0])}
+    line = {"mode": "sweeps", "qubits": n, "state_bytes": int(Ns), "steps": args.steps,
+            "warmup": args.warmup, "peak_hbm_gbs": peak["hbm_gbs"],
+            "peak_source": peak["source"], "sweeps": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        if args.impl == "reference":
+        if args.sweeps:
+            run_sweeps(args, dist)
+        elif args.impl == "reference":
             run_reference(args, dist)
         else:
             run_ours(args, dist)
