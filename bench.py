@@ -382,9 +382,11 @@ def run_ours(args, dist):
             b = s.amplitudes()
         parity = {"qubits": pn, "oracle": "FP64 (complex128) CPU oracle, same seed",
                   "fused": {"infidelity": infidelity(a, ref),
-                            "max_abs_err": float(np.max(np.abs(a - ref)))},
+                            "max_abs_err": float(np.max(np.abs(a - ref))),
+                            "norm_sq_minus_1": float(np.vdot(a, a).real - 1.0)},
                   "plain": {"infidelity": infidelity(b, ref),
-                            "max_abs_err": float(np.max(np.abs(b - ref)))}}
+                            "max_abs_err": float(np.max(np.abs(b - ref))),
+                            "norm_sq_minus_1": float(np.vdot(b, b).real - 1.0)}}
         cpu_rate = len(pg) / cpu_dt * 2.0 ** (pn - n)
         cpu = {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": (f"oracle (FP64, OpenMP over amplitude pairs) running the full "

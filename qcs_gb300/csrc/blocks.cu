@@ -28,7 +28,8 @@ int apply_ctrl(qcs_cuda_state *s, const double m[8], int c, int t);
 int phase_flip(qcs_cuda_state *s, i64 index);
 int diffusion(qcs_cuda_state *s);
 int check_qubit(const qcs_cuda_state *s, int q, const char *what);
-int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u);
+int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u,
+                   bool known_unitary);
 bool tc_supported(const qcs_cuda_state *s, int k);
 
 constexpr int kBlockThreads = 128;  // = max columns per tile
@@ -188,8 +189,9 @@ int apply_block(qcs_cuda_state *s, int k, const int *qubits, const double *u, in
   const bool tc_ok = tc_supported(s, k);
   if (engine == QCS_FUSE_TENSOR && strict && !tc_ok)
     return set_error(QCS_CUDA_EUNSUP, "tensor-core block engine: unsupported k=%d / precision", k);
+  // blocks from the planner (strict == false) are products of unitary gates
   if (tc_ok && (engine == QCS_FUSE_TENSOR || (engine == QCS_FUSE_AUTO && k > 4)))
-    return apply_block_tc(s, k, qubits, u);
+    return apply_block_tc(s, k, qubits, u, !strict);
   if (s->prec == QCS_CUDA_C128) return apply_block_simt_t<double2>(s, k, qubits, u);
   return apply_block_simt_t<float2>(s, k, qubits, u);
 }

@@ -9,32 +9,38 @@
 // of U[a'][a].  One tile is an M=128 (columns) x N=2^(k+1) (outputs) x
 // K=2^(k+1) (inputs) product on the 5th-generation tensor cores.
 //
-// Precision: split BF16.  Each state value x is held as hi = bf16(x),
-// lo = bf16(x - hi) (16 significant bits); each block-matrix entry as
-// hi + mid + lo (24 bits).  D = Ahi*Bhi + Ahi*Bmid + Ahi*Blo + Alo*Bhi,
-// accumulated in FP32 in tensor memory.  The state's representation error is
-// random from amplitude to amplitude; the matrix's is the same for every
-// column, so the matrix gets the third term: a 16-bit matrix makes the
-// applied operator non-unitary by ~1e-6 per block, a systematic norm drift
-// that 24 bits removes.
+// Precision: split BF16 x 3.  Every FP32 value x is held as hi = bf16(x),
+// lo = bf16(x - hi) (16 significant bits); D = Ahi*Bhi + Ahi*Blo + Alo*Bhi,
+// accumulated in FP32 in tensor memory.  The representation error is ~2^-17
+// per value and random in sign, so the direction error per block is ~1e-11
+// in infidelity.  The tensor cores' FP32 accumulation is not round-to-
+// nearest: chaining the K steps shrinks magnitudes by ~1e-6 per block, a
+// systematic norm drift (measured: 1 - p(0) = 1.2e-5 after 20 blocks at 30
+// qubits).  A unitary block preserves the norm of every column exactly, so
+// for unitary blocks the epilogue rescales each output column to the norm of
+// its input column (summed in FP32 by the producers), which removes the
+// drift; a non-unitary matrix passed to qcs_cuda_apply_block is applied
+// without that step.
 //
 // Kernel structure (persistent, one CTA per SM, 416 threads):
 //   warps 0-3   epilogue: tcgen05.ld the accumulator (warp w owns TMEM lanes
 //               32w..32w+31 = tile columns), store FP32 results to HBM;
 //   warps 4-11  producers: load the tile's amplitudes from HBM, split into
 //               bf16 hi/lo, write the 128-byte-swizzled K-major operand tile;
-//               (the block matrix stays resident in shared memory)
+//               the block matrix stays resident in shared memory; a
+//               producer issues its HBM loads before waiting for a free stage
 //   warp 12     TMEM allocation and MMA issue (one thread).
 // Operand tiles and TMEM accumulators are double buffered; stages hand over
 // through mbarriers.  Every wait is bounded: on expiry the kernel raises a
 // device error flag, all roles leave their loops, outstanding MMAs are
 // drained and TMEM is freed before exit.
 //
-// Shared memory (k = 6): 2 stages x (hi + lo) x 32 KB state tiles + 96 KB
-// block matrix (hi + mid + lo) + tables = 226.6 KB.  HBM traffic: one read
-// and one write of the state per block, the same as the SIMT engine; tensor
-// work per amplitude 4 x 8 x 2^k flops.
+// Shared memory (k = 6): 2 stages x (hi + lo) x 32 KB state tiles + 64 KB
+// block matrix (hi + lo) + tables ~= 197 KB.  HBM traffic: one read and one
+// write of the state per block, the same as the SIMT engine; tensor work per
+// amplitude 3 x 8 x 2^k flops.
 #include <cuda_bf16.h>
+#include <math.h>
 #include <string.h>
 
 #include <vector>
@@ -64,13 +70,14 @@ struct TcShape {
   static constexpr int UPT = UNITS / kTcProdThreads;
   static constexpr int TMEM_COLS = 2 * N;        // two accumulator stages
   static constexpr int OFF_A = 0;                // [stage][hi,lo][A_BYTES]
-  static constexpr int OFF_B = 4 * A_BYTES;      // [hi,mid,lo][B_BYTES]
-  static constexpr int OFF_COL = OFF_B + 3 * B_BYTES;
+  static constexpr int OFF_B = 4 * A_BYTES;      // [hi,lo][B_BYTES]
+  static constexpr int OFF_COL = OFF_B + 2 * B_BYTES;
   static constexpr int OFF_BLK = OFF_COL + kTcM * 8;
-  static constexpr int OFF_BAR = OFF_BLK + KA * 8;
+  static constexpr int OFF_SQ = OFF_BLK + KA * 8;  // float [stage][half][column]
+  static constexpr int OFF_BAR = OFF_SQ + 2 * 2 * kTcM * 4;
   static constexpr int OFF_MISC = OFF_BAR + 8 * 8;
   static constexpr int SMEM = OFF_MISC + 16 + 1024;  // + slack to align the base to 1 KB
-  static constexpr int IMG_BYTES = 3 * B_BYTES;
+  static constexpr int IMG_BYTES = 2 * B_BYTES;
   static_assert(SMEM <= 232448, "exceeds the 227 KB shared-memory opt-in");
   static_assert(UNITS % kTcProdThreads == 0, "tile units must split over producers");
   static_assert(KD % 64 == 0, "K extent must be whole 128-byte swizzle atoms");
@@ -223,7 +230,8 @@ __device__ __forceinline__ void unit_coords(int u, int &m, int &j) {
 
 template <int KA, bool COL_FAST>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_block_tc(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int *err) {
+    k_block_tc(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
+               int *err) {
   using S = TcShape<KA>;
   extern __shared__ uint8_t smem_dyn[];
   const uint32_t raw = smem_u32(smem_dyn);
@@ -232,6 +240,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint8_t *sB = smem + S::OFF_B;
   i64 *col_off = reinterpret_cast<i64 *>(smem + S::OFF_COL);
   i64 *blk_off = reinterpret_cast<i64 *>(smem + S::OFF_BLK);
+  float *colsq = reinterpret_cast<float *>(smem + S::OFF_SQ);
   const uint32_t bar0 = smem_u32(smem + S::OFF_BAR);  // 8-byte barriers:
   // 0,1 a_full[stage]  2,3 mma_done[stage]  4,5 acc_empty[stage]  6 drain
   auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
@@ -269,11 +278,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
   if (warp >= kTcEpiWarps && warp < kTcMmaWarp) {
     // ---------------- producers ----------------
+    // Stage reuse: the producer of tile it waits for the epilogue of tile
+    // it-2 (acc_empty), which implies the MMAs reading the stage are done and
+    // the stage's column norms have been consumed.
     const int p = tid - kTcEpiThreads;
     int it = 0;
     for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
       const int stage = it & 1;
-      if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
       const i64 base = tile_base(tile, g);
       float2 x[S::UPT][4];
 #pragma unroll
@@ -284,13 +295,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
         for (int e = 0; e < 4; e++) x[i][e] = src[blk_off[4 * j + e]];
       }
+      if (it >= 2 && !wait_bar(bar(4 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
       uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
       uint8_t *alo = ahi + S::A_BYTES;
+      float *sq = colsq + stage * 2 * kTcM;
+      float part_all = 0.f;
 #pragma unroll
       for (int i = 0; i < S::UPT; i++) {
         int m, j;
         unit_coords<KA, COL_FAST>(p + i * kTcProdThreads, m, j);
         uint32_t h[4], l[4];
+        float part = 0.f;
 #pragma unroll
         for (int e = 0; e < 4; e++) {
           __nv_bfloat162 hb = __floats2bfloat162_rn(x[i][e].x, x[i][e].y);
@@ -298,11 +313,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           __nv_bfloat162 lb = __floats2bfloat162_rn(x[i][e].x - hf.x, x[i][e].y - hf.y);
           h[e] = *reinterpret_cast<uint32_t *>(&hb);
           l[e] = *reinterpret_cast<uint32_t *>(&lb);
+          part += x[i][e].x * x[i][e].x + x[i][e].y * x[i][e].y;
         }
         const int off = sw128_offset(m, 8 * j, kTcM);
         *reinterpret_cast<uint4 *>(ahi + off) = make_uint4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<uint4 *>(alo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+        if (COL_FAST) {
+          part_all += part;  // every unit of this thread is in column p & 127
+        } else {
+          constexpr int G = KA / 4;  // consecutive lanes holding one column
+#pragma unroll
+          for (int o = G / 2; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+          if ((p & (G - 1)) == 0) {
+            sq[m] = part;
+            sq[kTcM + m] = 0.f;
+          }
+        }
       }
+      if (COL_FAST) sq[(p >> 7) * kTcM + (p & (kTcM - 1))] = part_all;
       fence_async_shared();
       mbar_arrive(bar(stage));
     }
@@ -310,8 +338,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // ---------------- MMA issue ----------------
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(kTcM, S::N);
-      const uint32_t a0 = smem_u32(sA), b_hi = smem_u32(sB);
-      const uint32_t b_mid = b_hi + S::B_BYTES, b_lo = b_mid + S::B_BYTES;
+      const uint32_t a0 = smem_u32(sA), b_hi = smem_u32(sB), b_lo = b_hi + S::B_BYTES;
       int it = 0;
       for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
         const int stage = it & 1;
@@ -326,7 +353,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const uint32_t ka = (uint32_t)((s >> 2) * (kTcM * 128) + (s & 3) * 32);
           const uint32_t kb = (uint32_t)((s >> 2) * (S::N * 128) + (s & 3) * 32);
           umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_hi + kb), idesc, s > 0 ? 1u : 0u);
-          umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_mid + kb), idesc, 1u);
           umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_lo + kb), idesc, 1u);
           umma_bf16(d, sw128_desc(a_lo + ka), sw128_desc(b_hi + kb), idesc, 1u);
         }
@@ -351,14 +377,33 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
       const int stage = it & 1;
       if (!wait_bar(bar(2 + stage), (it >> 1) & 1, abort_flag, err, 5)) break;
+      // the producer's column norms: a_full cannot have moved on, because the
+      // next producer of this stage waits for this epilogue
+      if (!wait_bar(bar(stage), (it >> 1) & 1, abort_flag, err, 6)) break;
       tc_fence_after();
+      const uint32_t tb = tmem + lane_addr + (uint32_t)(stage * S::N);
+      float scale = 1.f;
+      if (renorm) {
+        float out = 0.f;
+#pragma unroll 1
+        for (int c = 0; c < S::N / 32; c++) {
+          float acc[32];
+          tmem_ld32(tb + 32 * c, acc);
+#pragma unroll
+          for (int q = 0; q < 32; q++) out += acc[q] * acc[q];
+        }
+        const float *sq = colsq + stage * 2 * kTcM;
+        const float in = sq[m] + sq[kTcM + m];
+        if (out > 0.f) scale = sqrtf(in / out);
+      }
       float2 *dst = v + tile_base(tile, g) + col_off[m];
 #pragma unroll 1
       for (int c = 0; c < S::N / 32; c++) {
         float acc[32];
-        tmem_ld32(tmem + lane_addr + (uint32_t)(stage * S::N + 32 * c), acc);
+        tmem_ld32(tb + 32 * c, acc);
 #pragma unroll
-        for (int q = 0; q < 16; q++) dst[blk_off[16 * c + q]] = make_float2(acc[2 * q], acc[2 * q + 1]);
+        for (int q = 0; q < 16; q++)
+          dst[blk_off[16 * c + q]] = make_float2(acc[2 * q] * scale, acc[2 * q + 1] * scale);
       }
       tc_fence_before();
       mbar_arrive(bar(4 + stage));
@@ -399,14 +444,13 @@ static float bf16_to_float(uint16_t h) {
   return f;
 }
 
-// Block matrix u (K x K complex, row-major) -> swizzled hi/mid/lo image of B.
+// Block matrix u (K x K complex, row-major) -> swizzled hi/lo image of B.
 template <int KA>
 static void make_image(const double *u, uint8_t *img) {
   using S = TcShape<KA>;
   memset(img, 0, S::IMG_BYTES);
   uint16_t *hi = reinterpret_cast<uint16_t *>(img);
-  uint16_t *mid = reinterpret_cast<uint16_t *>(img + S::B_BYTES);
-  uint16_t *lo = reinterpret_cast<uint16_t *>(img + 2 * S::B_BYTES);
+  uint16_t *lo = reinterpret_cast<uint16_t *>(img + S::B_BYTES);
   for (int ao = 0; ao < KA; ao++)
     for (int ai = 0; ai < KA; ai++) {
       const double re = u[2 * (ao * KA + ai)], im = u[2 * (ao * KA + ai) + 1];
@@ -416,12 +460,9 @@ static void make_image(const double *u, uint8_t *img) {
           const int o = 2 * ao + co, i = 2 * ai + ci;
           const double x = blk[co][ci];
           const uint16_t h = bf16_rn((float)x);
-          const double r1 = x - (double)bf16_to_float(h);
-          const uint16_t m = bf16_rn((float)r1);
-          const uint16_t l = bf16_rn((float)(r1 - (double)bf16_to_float(m)));
+          const uint16_t l = bf16_rn((float)(x - (double)bf16_to_float(h)));
           const int off = sw128_offset(o, i, S::N) / 2;
           hi[off] = h;
-          mid[off] = m;
           lo[off] = l;
         }
     }
@@ -458,7 +499,7 @@ bool tc_supported(const qcs_cuda_state *s, int k) {
 }
 
 template <int KA, bool COL_FAST>
-static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img) {
+static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int renorm) {
   using S = TcShape<KA>;
   static bool configured = false;
   if (!configured) {
@@ -471,11 +512,31 @@ static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img) {
   const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
   prof_begin(s);
   k_block_tc<KA, COL_FAST><<<grid, kTcThreads, S::SMEM, s->stream>>>(
-      (float2 *)s->vec, g, img, s->d_err);
+      (float2 *)s->vec, g, img, renorm, s->d_err);
   return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
 }
 
-int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u) {
+// Largest |(U^H U - I)_ij|: unitary blocks get the per-column norm restore.
+static double unitarity_defect(const double *u, int K) {
+  double worst = 0.0;
+  for (int a = 0; a < K; a++)
+    for (int b = 0; b < K; b++) {
+      double re = 0.0, im = 0.0;
+      for (int r = 0; r < K; r++) {
+        const double ar = u[2 * (r * K + a)], ai = -u[2 * (r * K + a) + 1];
+        const double br = u[2 * (r * K + b)], bi = u[2 * (r * K + b) + 1];
+        re += ar * br - ai * bi;
+        im += ar * bi + ai * br;
+      }
+      if (a == b) re -= 1.0;
+      const double d = fabs(re) + fabs(im);
+      if (d > worst) worst = d;
+    }
+  return worst;
+}
+
+int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u,
+                   bool known_unitary) {
   int rc = ring_init(s);
   if (rc) return rc;
   TcRing *r = s->tc;
@@ -522,8 +583,11 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u)
                   "block image upload");
   if (rc) return rc;
   const uint4 *img = reinterpret_cast<const uint4 *>(d);
-  if (k == 6) rc = col_fast ? launch_tc<64, true>(s, g, img) : launch_tc<64, false>(s, g, img);
-  else rc = col_fast ? launch_tc<32, true>(s, g, img) : launch_tc<32, false>(s, g, img);
+  const int renorm = (known_unitary || unitarity_defect(u, KA) < 1e-9) ? 1 : 0;
+  if (k == 6)
+    rc = col_fast ? launch_tc<64, true>(s, g, img, renorm) : launch_tc<64, false>(s, g, img, renorm);
+  else
+    rc = col_fast ? launch_tc<32, true>(s, g, img, renorm) : launch_tc<32, false>(s, g, img, renorm);
   if (rc) return rc;
   return check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
 }

@@ -320,6 +320,25 @@ def test_apply_block_tensor_cores(k, with_q0):
             assert infidelity(a, b) < 1e-8
 
 
+def test_tensor_cores_preserve_the_norm_over_many_blocks():
+    """100 random 6-qubit unitaries: FP32 accumulation in the tensor cores
+    rounds toward zero; the per-column norm restore must keep the state's
+    norm to FP32 rounding."""
+    n = 16
+    rng = np.random.default_rng(77)
+    init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    init /= np.linalg.norm(init)
+    with capi.State(n, capi.C64) as s:
+        s.set_amplitudes(init)
+        for i in range(100):
+            m = rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64))
+            u, _ = np.linalg.qr(m)
+            qubits = list(rng.choice(n, size=6, replace=False))
+            s.apply_block(qubits, u, capi.FUSE_TENSOR)
+        s.synchronize()
+        assert abs(s.norm_sq() - 1.0) < 1e-5
+
+
 def test_tensor_engine_rejects_unsupported():
     with capi.State(12, capi.C128) as s:
         with pytest.raises(capi.QcsCudaError) as e:
