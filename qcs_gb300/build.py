@@ -26,7 +26,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["state.cu", "gates.cu", "readout.cu", "blocks.cu", "blocks_tc.cu",
-              "batch.cu", "mlp.cu"]
+              "batch.cu", "mlp.cu", "noalloc.cu"]
 CPP_SOURCES = ["fusion.cpp", "costmodel.cpp"]
 C_SOURCES = ["qcs_api.c"]
 

@@ -100,6 +100,7 @@ def _declare(L):
         "qcs_cuda_event_record": (i, [vp, vpp]),
         "qcs_cuda_event_elapsed": (i, [vp, vp, dp]),
         "qcs_cuda_event_destroy": (i, [vp]),
+        "qcs_cuda_sample_noalloc": (i, [vp, ll, i, vp, i, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
