@@ -58,6 +58,14 @@ def parse():
                     help="time each sweep type alone (HBM GB/s per kernel class)")
     ap.add_argument("--only", default=None,
                     help="with --sweeps: comma-separated subset of sweep types")
+    ap.add_argument("--workload", default="brick",
+                    choices=["brick", "random20", "grover", "batch", "learned"],
+                    help="brick: the headline 30-qubit brick circuit; random20: 20-qubit "
+                         "complex128 QFT + 200 random gates vs the reference rule; grover: "
+                         "QFT + 64 Grover iterations at --qubits (33/34); batch: 4096 "
+                         "variational instances in one persistent launch")
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--shots", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -494,12 +502,254 @@ def run_sweeps(args, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_random20(args, dist):
+    """20 qubits, complex128, random basis state, QFT, 200 random gates, one
+    kernel per gate.  REFERENCE semantics must equal the reference's
+    sequential rule (oracle COMPAT mode) bit for bit; PHYSICAL semantics must
+    equal the oracle's physical mode bit for bit."""
+    from oracle import oracle as O
+    from qcs_gb300 import build as B
+    from qcs_gb300 import capi
+    from qcs_gb300 import workloads as W
+    B.build()
+    O.build()
+    n = 20 if args.qubits == 30 else args.qubits
+    basis, g = W.random_circuit(n, args.seed, 200)
+    full = W.basis_gates(n, basis)
+    full.extend(g)
+    ops = full.ops()
+    out = {}
+    for name, sem, omode in (("reference", capi.REFERENCE, O.COMPAT),
+                             ("physical", capi.PHYSICAL, O.PHYSICAL)):
+        with capi.State(n, capi.C128, sem) as s:
+            for _ in range(args.warmup):
+                s.run(ops)
+            s.synchronize()
+            e0 = s.event()
+            for _ in range(args.steps):
+                s.run(ops)
+            e1 = s.event()
+            ms = capi.State.elapsed_ms(e0, e1) / args.steps
+            # a fresh run for the comparison
+        with capi.State(n, capi.C128, sem) as s:
+            s.run(ops)
+            a = s.amplitudes()
+        t0 = time.perf_counter()
+        with O.OracleState(n, omode) as o:
+            o.run(full)
+            ref = o.amplitudes()
+        cpu_s = time.perf_counter() - t0
+        out[name] = {"gate_apps_per_s": len(full) / (ms / 1e3), "ms_per_circuit": ms,
+                     "bit_exact": bool(np.array_equal(a.view(np.float64), ref.view(np.float64))),
+                     "max_abs_err": float(np.max(np.abs(a - ref))),
+                     "oracle_gate_apps_per_s": len(full) / cpu_s,
+                     "oracle_threads": os.cpu_count()}
+    line = {"mode": "random20", "qubits": n, "dtype": "complex128", "gates": len(full),
+            "seed": args.seed, "results": out,
+            "note": "REFERENCE compares against the oracle's COMPAT mode, which is "
+                    "bit-exact to the reference's sequential build (tests/golden)"}
+    print(json.dumps(line), flush=True)
+
+
+def run_grover(args, dist):
+    """QFT on a random basis state, a Hadamard layer, then 64 x (phase flip on a
+    random marked index, diffusion), complex64, at --qubits (33 or 34).
+    Reports HBM GB/s per sweep type from per-launch events, and checks argmax
+    and the marked probability against the FP64 oracle at --parity-qubits."""
+    from oracle import oracle as O
+    from qcs_gb300 import build as B
+    from qcs_gb300 import capi
+    from qcs_gb300 import workloads as W
+    B.build()
+    n = args.qubits
+    basis, marked, g = W.grover_workload(n, args.seed, iterations=64)
+    ops = g.ops()
+    res = {}
+    with capi.State(n, capi.C64) as s:
+        for k, label in ((0, "plain"), (args.fusion_k, "fused")):
+            s.set_basis(basis)
+            s.run(ops, fusion_k=k)  # warm-up
+            s.synchronize()
+            s.set_basis(basis)
+            s.profile(True)
+            e0 = s.event()
+            s.run(ops, fusion_k=k)
+            e1 = s.event()
+            ms = capi.State.elapsed_ms(e0, e1)
+            prof = s.profile_read()
+            s.profile(False)
+            res[label] = {"ms": ms, "ops_per_s": len(g) / (ms / 1e3),
+                          "by_kernel": {c: {"launches": v[0], "ms": v[1],
+                                            "GB/s": v[2] / (v[1] / 1e3) / 1e9}
+                                        for c, v in prof.items()}}
+        res["argmax"] = s.argmax()
+        res["marked"] = marked
+        res["p_marked"] = s.probability(marked)
+    parity = None
+    if not args.no_parity:
+        O.build()
+        pn = cpu_qubits(args.parity_qubits, buffers=1)
+        pb, pm, pg = W.grover_workload(pn, args.seed, iterations=64)
+        full = W.basis_gates(pn, pb)
+        full.extend(pg)
+        with O.OracleState(pn) as o:
+            o.run(full)
+            oarg, op = o.argmax(), o.probability(pm)
+        with capi.State(pn, capi.C64) as s:
+            s.run(full.ops(), fusion_k=args.fusion_k)
+            garg, gp = s.argmax(), s.probability(pm)
+        parity = {"qubits": pn, "argmax_gpu": garg, "argmax_fp64": oarg,
+                  "argmax_equal": garg == oarg, "p_marked_gpu": gp, "p_marked_fp64": op}
+    line = {"mode": "grover", "qubits": n, "state_bytes": 8 << n, "ops": len(g),
+            "results": res, "parity": parity}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(args, dist):
+    """4096 variational instances (n ~ U[10,22], depth ~ U[4,16] layers of RY/RZ
+    on every qubit plus a CNOT ladder), <Z_0> and 1024 shots each, one
+    persistent launch replayed from a CUDA graph with an autotuned schedule.
+    Instances shard across ranks (weak scaling, no collective)."""
+    from oracle import oracle as O
+    from qcs_gb300 import build as B
+    from qcs_gb300 import capi
+    from qcs_gb300 import workloads as W
+    B.build()
+    inst = W.variational_batch(args.instances, args.seed)
+    mine = inst[dist.rank::dist.world]
+    with capi.Batch(mine, shots=args.shots, seed=args.seed) as b:
+        tune = b.autotune(repeats=1)
+        for _ in range(args.warmup):
+            b.run()
+        dist.barrier()
+        times = []
+        for _ in range(args.steps):
+            z, samples, ms = b.run()
+            times.append(ms)
+        ms = dist.max(float(np.mean(times)))
+    check = None
+    if dist.rank == 0 and not args.no_parity:
+        O.build()
+        rng = np.random.default_rng(args.seed)
+        pick = rng.choice(len(mine), size=min(24, len(mine)), replace=False)
+        errs = []
+        for i in pick:
+            n, g = mine[i]
+            with O.OracleState(n) as o:
+                o.run(g)
+                errs.append(abs(o.expect_z(0) - z[i]))
+        check = {"instances_checked": len(pick), "max_abs_err_z0": float(max(errs)),
+                 "tolerance": 1e-5}
+    total_gates = sum(len(g) for _, g in inst)
+    line = {"mode": "batch", "instances": args.instances, "shots": args.shots,
+            "n_gpus": dist.world, "ms_per_batch": ms,
+            "instances_per_s": args.instances / (ms / 1e3),
+            "gate_apps_per_s": total_gates / (ms / 1e3), "schedule": tune,
+            "check": check, "scaling": "weak" if dist.world > 1 else None}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_learned(args, dist):
+    """Learned fusion cost model: ~20k kernel timings from random 24..32-qubit
+    circuits (every fusion width 2..6, both block engines), an MLP trained on
+    them by the library's own GPU kernels, then unseen 30-qubit depth-60 mixed
+    circuits (rotations, CNOTs, QFT-style controlled phases) timed three ways:
+    learned partition, greedy width-6 partition, unfused."""
+    from qcs_gb300 import build as B
+    from qcs_gb300 import capi
+    from qcs_gb300 import workloads as W
+    B.build()
+    rng = np.random.default_rng(args.seed)
+    feats, times = [], []
+    t_collect = time.perf_counter()
+    target = 20000
+    sizes = list(range(24, 33))
+    per_size = target // len(sizes)
+    for n in sizes:
+        got = 0
+        with capi.State(n, capi.C64) as s:
+            while got < per_size:
+                kind = rng.integers(3)
+                seed = int(rng.integers(1 << 30))
+                depth = int(rng.integers(2, 8))
+                g = (W.mixed_circuit(n, depth, seed) if kind == 0 else
+                     W.brick_circuit(n, depth, seed) if kind == 1 else
+                     W.random_circuit(n, seed, 40 * depth, with_qft=False)[1])
+                k = int(rng.integers(1, 7))
+                eng = capi.FUSE_SIMT if rng.random() < 0.3 else capi.FUSE_AUTO
+                f, ms = capi.collect_timings(s, g, kmax=k, engine=eng)
+                feats.append(f)
+                times.append(ms)
+                got += len(ms)
+    X = np.concatenate(feats)
+    Y = np.log2(np.maximum(np.concatenate(times), 1e-4)).astype(np.float32)
+    t_collect = time.perf_counter() - t_collect
+    perm = rng.permutation(len(Y))
+    X, Y = X[perm], Y[perm]
+    split = int(0.9 * len(Y))
+    model = capi.CostModel(seed=args.seed)
+    t_train = time.perf_counter()
+    train_loss = model.train(X[:split], Y[:split], epochs=60, batch=512, lr=2e-3)
+    t_train = time.perf_counter() - t_train
+    val = model.predict(X[split:])
+    val_mse = float(np.mean((val - Y[split:]) ** 2))
+    evals = []
+    n = args.qubits
+    with capi.State(n, capi.C64) as s:
+        s.set_costmodel(model)
+        for seed in (101, 202, 303):
+            g = W.mixed_circuit(n, 60, seed)
+            ops = g.ops()
+            row = {"seed": seed, "gates": len(g)}
+            for label, k, part in (("unfused", 0, capi.PARTITION_GREEDY),
+                                   ("greedy6", 6, capi.PARTITION_GREEDY),
+                                   ("learned", 6, capi.PARTITION_LEARNED)):
+                s.set_basis(0)
+                s.run(ops, fusion_k=k, partitioner=part)  # warm-up
+                ts = []
+                for _ in range(max(1, args.steps)):
+                    s.set_basis(0)
+                    e0 = s.event()
+                    s.run(ops, fusion_k=k, partitioner=part)
+                    e1 = s.event()
+                    ts.append(capi.State.elapsed_ms(e0, e1))
+                row[label + "_ms"] = float(np.median(ts))
+                if label != "unfused":
+                    row[label + "_state"] = s.amplitudes()
+            a, b = row.pop("learned_state"), row.pop("greedy6_state")
+            row["infidelity_learned_vs_greedy"] = float(
+                1.0 - abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real))
+            del a, b
+            plan = capi.plan_learned(g, n, 6, model)
+            row["learned_choice"] = plan["choice"]
+            row["pred_ms_learned"] = plan["pred_ms"]
+            row["pred_ms_greedy"] = plan["greedy_pred_ms"]
+            row["speedup_vs_greedy"] = row["greedy6_ms"] / row["learned_ms"]
+            row["speedup_vs_unfused"] = row["unfused_ms"] / row["learned_ms"]
+            evals.append(row)
+        s.set_costmodel(None)
+    model.close()
+    line = {"mode": "learned", "samples": int(len(Y)), "collect_s": t_collect,
+            "train_s": t_train, "train_mse": train_loss, "val_mse_log2ms": val_mse,
+            "eval_qubits": n, "eval": evals}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
         if args.sweeps:
             run_sweeps(args, dist)
+        elif args.workload == "random20":
+            run_random20(args, dist)
+        elif args.workload == "grover":
+            run_grover(args, dist)
+        elif args.workload == "batch":
+            run_batch(args, dist)
+        elif args.workload == "learned":
+            run_learned(args, dist)
         elif args.impl == "reference":
             run_reference(args, dist)
         else:

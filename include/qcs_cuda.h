@@ -202,6 +202,92 @@ int qcs_cuda_event_record(qcs_cuda_state *s, void **event);
 int qcs_cuda_event_elapsed(void *start, void *stop, double *ms);
 int qcs_cuda_event_destroy(void *event);
 
+/* ---- batched circuits ---------------------------------------------------
+ * Many independent circuits (1..26 qubits each) run by one persistent
+ * kernel, captured once into a CUDA graph and replayed.  Instance i has
+ * num_qubits[i] qubits and the gates ops[op_offsets[i] .. op_offsets[i+1]);
+ * the state starts at |0...0>.  Each run returns <Z_0> per instance (FP64
+ * accumulation) and `shots` samples per instance drawn from a counter-based
+ * generator keyed by (seed, instance, shot).  The reference has no batched
+ * form; per circuit this replaces qc_create + gates + the shot loop of
+ * qc_run_shots (src/qcs.c:575-607). */
+typedef struct qcs_cuda_batch qcs_cuda_batch;
+int qcs_cuda_batch_create(int count, const int *num_qubits,
+                          const int *op_offsets, const qcs_cuda_op *ops,
+                          int shots, unsigned long long seed,
+                          qcs_cuda_batch **out);
+int qcs_cuda_batch_destroy(qcs_cuda_batch *b);
+/* New angles for every op (in op order); the plan and graph are kept. */
+int qcs_cuda_batch_set_angles(qcs_cuda_batch *b, const double *angles);
+/* One replay.  expect_z0: `count` doubles; samples: count*shots indices
+ * (instance-major), may be NULL; ms: device time of the replay. */
+int qcs_cuda_batch_run(qcs_cuda_batch *b, double *expect_z0,
+                       long long *samples, double *ms);
+/* Times every schedule (threads per CTA 256/512/1024, tile 2^12..2^14,
+ * 1 or 2 CTAs per SM, largest-first or given order) on this batch and keeps
+ * the fastest; chosen (4 ints) receives it. */
+int qcs_cuda_batch_autotune(qcs_cuda_batch *b, int repeats, int *chosen);
+/* Sets one schedule explicitly. */
+int qcs_cuda_batch_config(qcs_cuda_batch *b, int threads, int tile_q,
+                          int ctas_per_sm, int order);
+
+/* ---- learned fusion cost model ------------------------------------------
+ * An MLP (QCS_COSTMODEL_FEATURES inputs, three hidden layers of 64 ReLU
+ * units, one output) that predicts log2 of a plan item's device time in ms.
+ * Forward, backward and Adam run on the GPU in this library's own kernels;
+ * the host keeps a copy of the weights for planning.  No reference
+ * counterpart (the reference has no fusion). */
+#define QCS_COSTMODEL_FEATURES 20
+typedef struct qcs_cuda_costmodel qcs_cuda_costmodel;
+int qcs_cuda_costmodel_create(int num_features, unsigned long long seed,
+                              qcs_cuda_costmodel **out);
+int qcs_cuda_costmodel_destroy(qcs_cuda_costmodel *m);
+int qcs_cuda_costmodel_num_params(qcs_cuda_costmodel *m, int *count);
+int qcs_cuda_costmodel_get_params(qcs_cuda_costmodel *m, float *out);
+int qcs_cuda_costmodel_set_params(qcs_cuda_costmodel *m, const float *in,
+                                  int count);
+/* Mean squared error over n samples (x: n x F row-major, y: n) and its
+ * gradient with respect to every parameter (grad may be NULL). */
+int qcs_cuda_costmodel_loss_grad(qcs_cuda_costmodel *m, const float *x,
+                                 const float *y, int n, double *loss,
+                                 float *grad);
+/* Adam, mini-batches of `batch` rows in the given order, `epochs` passes. */
+int qcs_cuda_costmodel_train(qcs_cuda_costmodel *m, const float *x,
+                             const float *y, int n, int epochs, int batch,
+                             float lr, double *final_loss);
+int qcs_cuda_costmodel_predict(qcs_cuda_costmodel *m, const float *x, int n,
+                               float *out);
+int qcs_cuda_costmodel_predict_host(qcs_cuda_costmodel *m, const float *x,
+                                    int n, float *out);
+/* Features of one plan item (category QCS_CAT_*, state qubits n, item
+ * qubits, gate count) into out[QCS_COSTMODEL_FEATURES]. */
+#define QCS_CAT_DENSE 0
+#define QCS_CAT_DIAG 1
+#define QCS_CAT_PHASE 2
+#define QCS_CAT_CTRL 3
+#define QCS_CAT_CPHASE 4
+#define QCS_CAT_SIMT 5
+#define QCS_CAT_TC 6
+int qcs_cuda_item_features(int category, int n, int k, const int *qubits,
+                           int ngates, float *out);
+/* Run ops[0..count) on the state with fusion width kmax and `engine`, timing
+ * every plan item with CUDA events: features (max x F) and milliseconds
+ * (max) of up to `max` items; *written receives how many. */
+int qcs_cuda_collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops,
+                             int count, int kmax, int engine, float *features,
+                             float *ms, int max, int *written);
+/* The model qcs_cuda_run uses when options.partitioner is
+ * QCS_PARTITION_LEARNED (NULL detaches it; the greedy plan is then used). */
+int qcs_cuda_state_set_costmodel(qcs_cuda_state *s, qcs_cuda_costmodel *m);
+/* Host only: the learned plan for a num_qubits state (order/item as in
+ * qcs_cuda_plan), the model's predicted ms for it and for the greedy
+ * width-kmax plan, and which candidate won (2..7: greedy width; 100 + k:
+ * model-stopped growth at width k). */
+int qcs_cuda_plan_learned(const qcs_cuda_op *ops, int count, int num_qubits,
+                          int kmax, qcs_cuda_costmodel *m, int *order,
+                          int *item, int *num_items, double *pred_ms,
+                          double *greedy_ms, int *choice);
+
 /* ---- reductions and read-out (FP64 accumulation) ----------------------- */
 int qcs_cuda_norm_sq(qcs_cuda_state *s, double *out);
 /* q_state_normalize (src/q_utils.c:44-119): rescale when the norm^2 is

@@ -64,6 +64,7 @@ def _declare(L):
     vp, i, d, ll = C.c_void_p, C.c_int, C.c_double, C.c_longlong
     dp, ip, llp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_longlong)
     vpp = C.POINTER(C.c_void_p)
+    fp = C.POINTER(C.c_float)
     sig = {
         "qcs_cuda_strerror": (C.c_char_p, [i]),
         "qcs_cuda_last_error": (C.c_char_p, []),
@@ -101,6 +102,25 @@ def _declare(L):
         "qcs_cuda_event_elapsed": (i, [vp, vp, dp]),
         "qcs_cuda_event_destroy": (i, [vp]),
         "qcs_cuda_sample_noalloc": (i, [vp, ll, i, vp, i, vp, vp]),
+        "qcs_cuda_batch_create": (i, [i, ip, ip, vp, i, C.c_ulonglong, vpp]),
+        "qcs_cuda_batch_destroy": (i, [vp]),
+        "qcs_cuda_batch_set_angles": (i, [vp, dp]),
+        "qcs_cuda_batch_run": (i, [vp, dp, llp, dp]),
+        "qcs_cuda_batch_autotune": (i, [vp, i, ip]),
+        "qcs_cuda_batch_config": (i, [vp, i, i, i, i]),
+        "qcs_cuda_costmodel_create": (i, [i, C.c_ulonglong, vpp]),
+        "qcs_cuda_costmodel_destroy": (i, [vp]),
+        "qcs_cuda_costmodel_num_params": (i, [vp, ip]),
+        "qcs_cuda_costmodel_get_params": (i, [vp, fp]),
+        "qcs_cuda_costmodel_set_params": (i, [vp, fp, i]),
+        "qcs_cuda_costmodel_loss_grad": (i, [vp, fp, fp, i, dp, fp]),
+        "qcs_cuda_costmodel_train": (i, [vp, fp, fp, i, i, i, C.c_float, dp]),
+        "qcs_cuda_costmodel_predict": (i, [vp, fp, i, fp]),
+        "qcs_cuda_costmodel_predict_host": (i, [vp, fp, i, fp]),
+        "qcs_cuda_item_features": (i, [i, i, i, ip, i, fp]),
+        "qcs_cuda_collect_timings": (i, [vp, vp, i, i, i, fp, fp, i, ip]),
+        "qcs_cuda_state_set_costmodel": (i, [vp, vp]),
+        "qcs_cuda_plan_learned": (i, [vp, i, i, i, vp, ip, ip, ip, dp, dp, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -291,6 +311,9 @@ class State:
         lib().qcs_cuda_event_destroy(stop)
         return ms.value
 
+    def set_costmodel(self, model):
+        _check(lib().qcs_cuda_state_set_costmodel(self._h, model.handle if model else None))
+
     def launch_count(self) -> int:
         n = C.c_longlong()
         _check(lib().qcs_cuda_launch_count(self._h, C.byref(n)))
@@ -315,6 +338,168 @@ def plan(gates, n: int, kmax: int):
                                order.ctypes.data_as(ipp), item.ctypes.data_as(ipp),
                                C.byref(cnt)))
     return order, item, cnt.value
+
+
+class Batch:
+    """Many circuits in one persistent kernel (qcs_cuda_batch_*)."""
+
+    def __init__(self, instances, shots: int = 1024, seed: int = 1):
+        """instances: list of (num_qubits, GateList)."""
+        self.count = len(instances)
+        self.shots = shots
+        nq = np.array([n for n, _ in instances], dtype=np.int32)
+        offs = np.zeros(self.count + 1, dtype=np.int32)
+        chunks = []
+        for i, (_, g) in enumerate(instances):
+            ops = g.ops()
+            chunks.append(ops)
+            offs[i + 1] = offs[i] + len(ops)
+        self.ops = np.concatenate(chunks) if chunks else np.zeros(0, dtype=W.OP_DTYPE)
+        h = C.c_void_p()
+        ipp = C.POINTER(C.c_int)
+        _check(lib().qcs_cuda_batch_create(self.count, nq.ctypes.data_as(ipp),
+                                           offs.ctypes.data_as(ipp),
+                                           self.ops.ctypes.data_as(C.c_void_p), shots,
+                                           C.c_ulonglong(seed), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().qcs_cuda_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, want_samples: bool = True):
+        """(<Z_0> per instance, samples [count, shots] or None, device ms)."""
+        z = np.zeros(self.count, dtype=np.float64)
+        samples = np.zeros((self.count, self.shots), dtype=np.int64) if want_samples else None
+        ms = C.c_double()
+        _check(lib().qcs_cuda_batch_run(
+            self._h, _dp(z),
+            samples.ctypes.data_as(C.POINTER(C.c_longlong)) if samples is not None else None,
+            C.byref(ms)))
+        return z, samples, ms.value
+
+    def set_angles(self, angles: np.ndarray):
+        a = np.ascontiguousarray(angles, dtype=np.float64)
+        assert len(a) == len(self.ops)
+        _check(lib().qcs_cuda_batch_set_angles(self._h, _dp(a)))
+
+    def autotune(self, repeats: int = 2):
+        out = (C.c_int * 4)()
+        _check(lib().qcs_cuda_batch_autotune(self._h, repeats, out))
+        return {"threads": out[0], "tile_q": out[1], "ctas_per_sm": out[2],
+                "order": "largest-first" if out[3] == 0 else "given"}
+
+    def config(self, threads: int, tile_q: int, ctas_per_sm: int, order: int = 0):
+        _check(lib().qcs_cuda_batch_config(self._h, threads, tile_q, ctas_per_sm, order))
+
+
+COSTMODEL_FEATURES = 20
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class CostModel:
+    """The learned fusion cost model (qcs_cuda_costmodel_*)."""
+
+    def __init__(self, seed: int = 1, features: int = COSTMODEL_FEATURES):
+        self.F = features
+        h = C.c_void_p()
+        _check(lib().qcs_cuda_costmodel_create(features, C.c_ulonglong(seed), C.byref(h)))
+        self._h = h
+        n = C.c_int()
+        _check(lib().qcs_cuda_costmodel_num_params(h, C.byref(n)))
+        self.num_params = n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().qcs_cuda_costmodel_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, dtype=np.float32)
+        _check(lib().qcs_cuda_costmodel_get_params(self._h, _fp(out)))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(lib().qcs_cuda_costmodel_set_params(self._h, _fp(p), len(p)))
+
+    def loss_grad(self, x: np.ndarray, y: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.zeros(self.num_params, dtype=np.float32)
+        loss = C.c_double()
+        _check(lib().qcs_cuda_costmodel_loss_grad(self._h, _fp(x), _fp(y), len(y), C.byref(loss),
+                                                  _fp(g)))
+        return loss.value, g
+
+    def train(self, x, y, epochs=30, batch=256, lr=1e-3) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        loss = C.c_double()
+        _check(lib().qcs_cuda_costmodel_train(self._h, _fp(x), _fp(y), len(y), epochs, batch,
+                                              C.c_float(lr), C.byref(loss)))
+        return loss.value
+
+    def predict(self, x, host: bool = False) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.zeros(len(x), dtype=np.float32)
+        f = lib().qcs_cuda_costmodel_predict_host if host else lib().qcs_cuda_costmodel_predict
+        _check(f(self._h, _fp(x), len(x), _fp(out)))
+        return out
+
+
+def collect_timings(state: "State", gates, kmax: int, engine: int = FUSE_AUTO, max_items=100000):
+    """(features [m, F], device ms [m]) of every plan item of `gates`."""
+    ops = gates.ops() if isinstance(gates, W.GateList) else np.ascontiguousarray(gates)
+    feats = np.zeros((max_items, COSTMODEL_FEATURES), dtype=np.float32)
+    ms = np.zeros(max_items, dtype=np.float32)
+    n = C.c_int()
+    _check(lib().qcs_cuda_collect_timings(state.handle, ops.ctypes.data_as(C.c_void_p), len(ops),
+                                          kmax, engine, _fp(feats), _fp(ms), max_items,
+                                          C.byref(n)))
+    return feats[:n.value], ms[:n.value]
+
+
+def plan_learned(gates, n: int, kmax: int, model: CostModel):
+    ops = gates.ops() if isinstance(gates, W.GateList) else np.ascontiguousarray(gates)
+    order = np.zeros(len(ops), dtype=np.int32)
+    item = np.zeros(len(ops), dtype=np.int32)
+    cnt = C.c_int()
+    pred, greedy = C.c_double(), C.c_double()
+    choice = C.c_int()
+    ipp = C.POINTER(C.c_int)
+    _check(lib().qcs_cuda_plan_learned(ops.ctypes.data_as(C.c_void_p), len(ops), n, kmax,
+                                       model.handle, order.ctypes.data_as(ipp),
+                                       item.ctypes.data_as(ipp), C.byref(cnt), C.byref(pred),
+                                       C.byref(greedy), C.byref(choice)))
+    return {"order": order, "item": item, "items": cnt.value, "pred_ms": pred.value,
+            "greedy_pred_ms": greedy.value, "choice": choice.value}
 
 
 _api = None

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "costmodel.h"
 #include "fusion.h"
 
 namespace qcs {
@@ -224,6 +225,28 @@ static int apply_op(qcs_cuda_state *s, const qcs_cuda_op &o) {
   return apply_1q(s, m, o.target);
 }
 
+static int apply_item(qcs_cuda_state *s, const qcs_cuda_op *ops, const PlanItem &it, int engine,
+                      std::vector<cd> &u) {
+  if (it.kind == 1) return apply_op(s, ops[it.op]);
+  if (it.gates.size() == 1) return apply_op(s, ops[it.gates[0]]);
+  block_matrix(ops, it, u);
+  const int kb = (int)it.qubits.size();
+  if (kb == 1) {
+    double m[8] = {u[0].real(), u[0].imag(), u[1].real(), u[1].imag(),
+                   u[2].real(), u[2].imag(), u[3].real(), u[3].imag()};
+    return apply_1q(s, m, it.qubits[0]);
+  }
+  return apply_block(s, kb, it.qubits.data(), reinterpret_cast<const double *>(u.data()), engine,
+                     false);
+}
+
+static int fusion_cap(const qcs_cuda_state *s, int k, int engine) {
+  int kcap = (engine != QCS_FUSE_SIMT && tc_supported(s, 6)) ? 6 : kSimtMaxK;
+  if (k > kcap) k = kcap;
+  if (k > s->n) k = s->n;
+  return k;
+}
+
 int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda_run_options *opt) {
   int rc = validate_ops(s, ops, count);
   if (rc) return rc;
@@ -235,36 +258,73 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
     }
     return QCS_CUDA_OK;
   }
-  int engine = opt->fusion_engine;
-  int kcap = (engine != QCS_FUSE_SIMT && tc_supported(s, 6)) ? 6 : kSimtMaxK;
-  if (k > kcap) k = kcap;
-  if (k > s->n) k = s->n;
-  PartitionOptions po;
-  po.kmax = k;
-  po.cost = nullptr;
-  po.cost_ctx = nullptr;
-  std::vector<PlanItem> plan = partition(ops, count, s->n, po);
+  const int engine = opt->fusion_engine;
+  k = fusion_cap(s, k, engine);
+  std::vector<PlanItem> plan;
+  if (opt->partitioner == QCS_PARTITION_LEARNED && costmodel_ready(s->cm)) {
+    const bool simt_only = engine == QCS_FUSE_SIMT;
+    plan = partition_learned(ops, count, s->n, k, s->cm, !simt_only && tc_supported(s, 5),
+                             !simt_only && tc_supported(s, 6), nullptr, nullptr, nullptr);
+  } else {
+    PartitionOptions po;
+    po.kmax = k;
+    po.cost = nullptr;
+    po.cost_ctx = nullptr;
+    plan = partition(ops, count, s->n, po);
+  }
   std::vector<cd> u;
   for (const PlanItem &it : plan) {
-    if (it.kind == 1) {
-      rc = apply_op(s, ops[it.op]);
-    } else if (it.gates.size() == 1) {
-      rc = apply_op(s, ops[it.gates[0]]);
-    } else {
-      block_matrix(ops, it, u);
-      const int kb = (int)it.qubits.size();
-      if (kb == 1) {
-        double m[8] = {u[0].real(), u[0].imag(), u[1].real(), u[1].imag(),
-                       u[2].real(), u[2].imag(), u[3].real(), u[3].imag()};
-        rc = apply_1q(s, m, it.qubits[0]);
-      } else {
-        rc = apply_block(s, kb, it.qubits.data(), reinterpret_cast<const double *>(u.data()), engine,
-                         false);
-      }
-    }
+    rc = apply_item(s, ops, it, engine, u);
     if (rc) return rc;
   }
   return QCS_CUDA_OK;
+}
+
+int collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, int kmax, int engine,
+                    float *feats, float *ms, int max, int *written) {
+  int rc = validate_ops(s, ops, count);
+  if (rc) return rc;
+  kmax = fusion_cap(s, kmax < 1 ? 1 : kmax, engine);
+  PartitionOptions po;
+  po.kmax = kmax;
+  po.cost = nullptr;
+  po.cost_ctx = nullptr;
+  std::vector<PlanItem> plan = partition(ops, count, s->n, po);
+  const bool tc5 = engine != QCS_FUSE_SIMT && tc_supported(s, 5);
+  const bool tc6 = engine != QCS_FUSE_SIMT && tc_supported(s, 6);
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> rec;  // item index of each recorded pair
+  std::vector<cd> u;
+  for (size_t i = 0; i < plan.size(); i++) {
+    const bool timed = plan[i].kind == 0 && (int)rec.size() < max;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (timed) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, s->stream);
+    }
+    rc = apply_item(s, ops, plan[i], engine, u);
+    if (timed) {
+      cudaEventRecord(b, s->stream);
+      ev.push_back(a);
+      ev.push_back(b);
+      rec.push_back((int)i);
+    }
+    if (rc) break;
+  }
+  if (!rc) rc = check_cuda(cudaStreamSynchronize(s->stream), "collect sync");
+  for (size_t r = 0; r < rec.size(); r++) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ev[2 * r], ev[2 * r + 1]);
+    const PlanItem &it = plan[rec[r]];
+    const int cat = item_category(ops, it, tc5, tc6);
+    item_features(cat, s->n, (int)it.qubits.size(), (int)it.gates.size(), it.qubits.data(),
+                  feats + r * kCostFeatures);
+    ms[r] = t;
+  }
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  if (written) *written = (int)rec.size();
+  return rc;
 }
 
 }  // namespace qcs
@@ -306,6 +366,62 @@ int qcs_cuda_plan(const qcs_cuda_op *ops, int count, int num_qubits, int kmax, i
   po.cost = nullptr;
   po.cost_ctx = nullptr;
   std::vector<PlanItem> plan = partition(ops, count, num_qubits, po);
+  int j = 0;
+  for (size_t it = 0; it < plan.size(); it++) {
+    if (plan[it].kind == 1) {
+      order[j] = plan[it].op;
+      item[j++] = (int)it;
+    } else {
+      for (int g : plan[it].gates) {
+        order[j] = g;
+        item[j++] = (int)it;
+      }
+    }
+  }
+  *num_items = (int)plan.size();
+  return QCS_CUDA_OK;
+}
+
+int qcs_cuda_collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, int kmax,
+                             int engine, float *features, float *ms, int max, int *written) {
+  QCS_CHECK_STATE(s);
+  if (count < 0 || (count > 0 && !ops) || max < 0 || (max > 0 && (!features || !ms)))
+    return set_error(QCS_CUDA_EINVAL, "bad collect arguments");
+  return collect_timings(s, ops, count, kmax, engine, features, ms, max, written);
+}
+
+int qcs_cuda_state_set_costmodel(qcs_cuda_state *s, qcs_cuda_costmodel *m) {
+  QCS_CHECK_STATE(s);
+  if (m && costmodel_features(m) != kCostFeatures)
+    return set_error(QCS_CUDA_EINVAL, "cost model must take %d features", kCostFeatures);
+  s->cm = m;
+  return QCS_CUDA_OK;
+}
+
+int qcs_cuda_item_features(int category, int n, int k, const int *qubits, int ngates, float *out) {
+  if (category < 0 || category > 6 || k < 1 || k > 8 || !qubits || !out)
+    return set_error(QCS_CUDA_EINVAL, "bad item");
+  item_features(category, n, k, ngates, qubits, out);
+  return QCS_CUDA_OK;
+}
+
+int qcs_cuda_plan_learned(const qcs_cuda_op *ops, int count, int num_qubits, int kmax,
+                          qcs_cuda_costmodel *m, int *order, int *item, int *num_items,
+                          double *pred_ms, double *greedy_ms, int *choice) {
+  if (count < 0 || (count > 0 && (!ops || !order || !item)) || !num_items || !m)
+    return set_error(QCS_CUDA_EINVAL, "bad plan arguments");
+  if (!costmodel_ready(m) || costmodel_features(m) != kCostFeatures)
+    return set_error(QCS_CUDA_EINVAL, "cost model not ready");
+  qcs_cuda_state shape;
+  memset(&shape, 0, sizeof(shape));
+  shape.n = num_qubits;
+  shape.size = 1LL << num_qubits;
+  int rc = validate_ops(&shape, ops, count);
+  if (rc) return rc;
+  if (kmax > 6) kmax = 6;
+  std::vector<PlanItem> plan =
+      partition_learned(ops, count, num_qubits, kmax, m, num_qubits >= 12, num_qubits >= 13,
+                        pred_ms, greedy_ms, choice);
   int j = 0;
   for (size_t it = 0; it < plan.size(); it++) {
     if (plan[it].kind == 1) {

@@ -58,6 +58,7 @@ constexpr int kTcProdThreads = kTcProdWarps * 32;        // 256
 constexpr int kTcEpiThreads = kTcEpiWarps * 32;          // 128
 constexpr long long kWaitCycles = 4000000000LL;          // ~2 s at 2 GHz
 constexpr int kImgSlots = 8;                             // block-matrix upload ring
+constexpr int kSqSlots = 4;                              // column-norm ring
 
 template <int KA>  // amplitudes per column (2^k)
 struct TcShape {
@@ -73,9 +74,9 @@ struct TcShape {
   static constexpr int OFF_B = 4 * A_BYTES;      // [hi,lo][B_BYTES]
   static constexpr int OFF_COL = OFF_B + 2 * B_BYTES;
   static constexpr int OFF_BLK = OFF_COL + kTcM * 8;
-  static constexpr int OFF_SQ = OFF_BLK + KA * 8;  // float [stage][half][column]
-  static constexpr int OFF_BAR = OFF_SQ + 2 * 2 * kTcM * 4;
-  static constexpr int OFF_MISC = OFF_BAR + 8 * 8;
+  static constexpr int OFF_SQ = OFF_BLK + KA * 8;  // float [slot 4][half][column]
+  static constexpr int OFF_BAR = OFF_SQ + kSqSlots * 2 * kTcM * 4;
+  static constexpr int OFF_MISC = OFF_BAR + 12 * 8;
   static constexpr int SMEM = OFF_MISC + 16 + 1024;  // + slack to align the base to 1 KB
   static constexpr int IMG_BYTES = 2 * B_BYTES;
   static_assert(SMEM <= 232448, "exceeds the 227 KB shared-memory opt-in");
@@ -243,6 +244,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   float *colsq = reinterpret_cast<float *>(smem + S::OFF_SQ);
   const uint32_t bar0 = smem_u32(smem + S::OFF_BAR);  // 8-byte barriers:
   // 0,1 a_full[stage]  2,3 mma_done[stage]  4,5 acc_empty[stage]  6 drain
+  // 7..10 sq_full[slot]: a tile's column norms are in colsq[slot]
   auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::OFF_MISC);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::OFF_MISC + 4);
@@ -257,6 +259,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     mbar_init(bar(4), kTcEpiThreads);
     mbar_init(bar(5), kTcEpiThreads);
     mbar_init(bar(6), 1);
+    for (int k = 0; k < kSqSlots; k++) mbar_init(bar(7 + k), kTcProdThreads);
     *abort_flag = 0;
     fence_barrier_init();
   }
@@ -278,9 +281,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
   if (warp >= kTcEpiWarps && warp < kTcMmaWarp) {
     // ---------------- producers ----------------
-    // Stage reuse: the producer of tile it waits for the epilogue of tile
-    // it-2 (acc_empty), which implies the MMAs reading the stage are done and
-    // the stage's column norms have been consumed.
+    // Stage reuse: the producer of tile it waits for the MMAs of tile it-2.
+    // Column-norm slot it % 4 was last read by the epilogue of tile it-4,
+    // which finished before the MMAs of tile it-2 could start (they wait for
+    // its acc_empty), so the slot is free too.
     const int p = tid - kTcEpiThreads;
     int it = 0;
     for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
@@ -295,10 +299,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
         for (int e = 0; e < 4; e++) x[i][e] = src[blk_off[4 * j + e]];
       }
-      if (it >= 2 && !wait_bar(bar(4 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
+      if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
       uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
       uint8_t *alo = ahi + S::A_BYTES;
-      float *sq = colsq + stage * 2 * kTcM;
+      float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
       float part_all = 0.f;
 #pragma unroll
       for (int i = 0; i < S::UPT; i++) {
@@ -333,6 +337,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (COL_FAST) sq[(p >> 7) * kTcM + (p & (kTcM - 1))] = part_all;
       fence_async_shared();
       mbar_arrive(bar(stage));
+      mbar_arrive(bar(7 + it % kSqSlots));
     }
   } else if (warp == kTcMmaWarp) {
     // ---------------- MMA issue ----------------
@@ -377,9 +382,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
       const int stage = it & 1;
       if (!wait_bar(bar(2 + stage), (it >> 1) & 1, abort_flag, err, 5)) break;
-      // the producer's column norms: a_full cannot have moved on, because the
-      // next producer of this stage waits for this epilogue
-      if (!wait_bar(bar(stage), (it >> 1) & 1, abort_flag, err, 6)) break;
+      // this tile's column norms; slot it % 4 cannot be refilled before this
+      // epilogue arrives on acc_empty, so its phase is unambiguous
+      if (!wait_bar(bar(7 + it % kSqSlots), (it / kSqSlots) & 1, abort_flag, err, 6)) break;
       tc_fence_after();
       const uint32_t tb = tmem + lane_addr + (uint32_t)(stage * S::N);
       float scale = 1.f;
@@ -392,7 +397,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
           for (int q = 0; q < 32; q++) out += acc[q] * acc[q];
         }
-        const float *sq = colsq + stage * 2 * kTcM;
+        const float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
         const float in = sq[m] + sq[kTcM + m];
         if (out > 0.f) scale = sqrtf(in / out);
       }

@@ -84,6 +84,7 @@ struct qcs_cuda_state {
   qcs::ProfData *prof;    // non-null while profiling
   qcs::TcRing *tc;        // created on first tensor-core block
   int *d_err;             // device error flag (bounded waits that gave up)
+  qcs_cuda_costmodel *cm; // model for QCS_PARTITION_LEARNED (not owned)
 };
 
 namespace qcs {

@@ -1,1 +1,147 @@
-// costmodel.cpp -- learned fusion cost model, host side (placeholder).
+// costmodel.cpp -- features of plan items and the learned partitioner.
+//
+// The greedy fixed-k planner (fusion.cpp) fuses as wide as k allows.  Wider
+// is not always faster: a 5-qubit block on the CUDA cores is FP32-bound, a
+// lone diagonal gate touches half the state, the tensor-core engine has a
+// per-launch cost.  A small MLP trained on timings of this simulator's own
+// kernels predicts each item's device time from the features below; the
+// learned partitioner scores several candidate plans with it and keeps the
+// cheapest, with the greedy width-k plan as the fallback and the judge.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "costmodel.h"
+
+namespace qcs {
+
+void item_features(int cat, int n, int k, int ngates, const int *qubits, float *f) {
+  memset(f, 0, kCostFeatures * sizeof(float));
+  f[cat] = 1.f;
+  f[7] = n / 32.f;
+  f[8] = k / 8.f;
+  f[9] = ngates / 64.f;
+  int low = 0, top = 0;
+  for (int j = 0; j < k; j++) {
+    const int q = qubits[j];
+    if (q < 8) f[10 + q] = 1.f;
+    if (q < 7) low++;
+    if (q > top) top = q;
+  }
+  f[18] = low / 7.f;
+  f[19] = top / 32.f;
+}
+
+static bool is_zero(const double *z) { return z[0] == 0.0 && z[1] == 0.0; }
+static bool is_one(const double *z) { return z[0] == 1.0 && z[1] == 0.0; }
+
+int item_category(const qcs_cuda_op *ops, const PlanItem &it, bool tc_ok_5, bool tc_ok_6) {
+  const int k = (int)it.qubits.size();
+  if (it.gates.size() == 1 || k == 1) {
+    // a single gate, or a product of one-qubit gates on one qubit: plain kernel
+    double m[8];
+    int kind = ops[it.gates[0]].kind;
+    bool ctl = gate_is_controlled(kind);
+    if (it.gates.size() == 1) {
+      gate_matrix(kind, ops[it.gates[0]].angle, m);
+    } else {
+      // product of the 2x2s (same qubit): classify the result
+      double a[8] = {1, 0, 0, 0, 0, 0, 1, 0};
+      for (int g : it.gates) {
+        double b[8], r[8];
+        gate_matrix(ops[g].kind, ops[g].angle, b);
+        for (int i = 0; i < 2; i++)
+          for (int j = 0; j < 2; j++) {
+            double re = 0, im = 0;
+            for (int l = 0; l < 2; l++) {
+              const double *x = b + 2 * (2 * i + l), *y = a + 2 * (2 * l + j);
+              re += x[0] * y[0] - x[1] * y[1];
+              im += x[0] * y[1] + x[1] * y[0];
+            }
+            r[2 * (2 * i + j)] = re;
+            r[2 * (2 * i + j) + 1] = im;
+          }
+        memcpy(a, r, sizeof(a));
+      }
+      memcpy(m, a, sizeof(a));
+    }
+    const bool diag = is_zero(m + 2) && is_zero(m + 4);
+    if (ctl) return (diag && is_one(m)) ? CAT_CPHASE : CAT_CTRL;
+    if (diag && is_one(m)) return CAT_PHASE;
+    if (diag) return CAT_DIAG;
+    return CAT_DENSE;
+  }
+  if ((k == 5 && tc_ok_5) || (k == 6 && tc_ok_6)) return CAT_TC;
+  return CAT_SIMT;
+}
+
+struct PlanScore {
+  const qcs_cuda_costmodel *m;
+  const qcs_cuda_op *ops;
+  int n;
+  bool tc5, tc6;
+};
+
+static double item_ms(const PlanScore &ps, const PlanItem &it) {
+  if (it.kind == 1) return 0.0;  // non-gate ops are the same in every plan
+  float f[kCostFeatures];
+  const int cat = item_category(ps.ops, it, ps.tc5, ps.tc6);
+  item_features(cat, ps.n, (int)it.qubits.size(), (int)it.gates.size(), it.qubits.data(), f);
+  return exp2((double)costmodel_predict_host(ps.m, f));
+}
+
+static double plan_ms(const PlanScore &ps, const std::vector<PlanItem> &plan) {
+  double t = 0.0;
+  for (const PlanItem &it : plan) t += item_ms(ps, it);
+  return t;
+}
+
+// Growth hook: predicted time of a block of k qubits and ngates gates.
+static double grow_cost(int n, int k, int ngates, const int *qubits, void *ctx) {
+  const PlanScore &ps = *static_cast<const PlanScore *>(ctx);
+  int cat;
+  if (k == 1) cat = CAT_DENSE;
+  else if ((k == 5 && ps.tc5) || (k == 6 && ps.tc6)) cat = CAT_TC;
+  else cat = CAT_SIMT;
+  float f[kCostFeatures];
+  item_features(cat, n, k, ngates, qubits, f);
+  return exp2((double)costmodel_predict_host(ps.m, f));
+}
+
+std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n, int kmax,
+                                        const qcs_cuda_costmodel *m, bool tc_ok_5,
+                                        bool tc_ok_6, double *pred_ms, double *greedy_ms,
+                                        int *choice) {
+  PlanScore ps{m, ops, n, tc_ok_5, tc_ok_6};
+  PartitionOptions po;
+  po.kmax = kmax;
+  po.cost = nullptr;
+  po.cost_ctx = nullptr;
+  std::vector<PlanItem> best = partition(ops, count, n, po);
+  const double judge = plan_ms(ps, best);
+  double best_ms = judge;
+  int best_choice = kmax;  // 2..7: greedy width; 100 + k: model-stopped growth
+  for (int k = 2; k <= kmax; k++) {
+    // greedy at a smaller width, and model-stopped growth at each width
+    for (int grown = 0; grown < 2; grown++) {
+      if (!grown && k == kmax) continue;
+      po.kmax = k;
+      po.cost = grown ? grow_cost : nullptr;
+      po.cost_ctx = grown ? &ps : nullptr;
+      std::vector<PlanItem> cand = partition(ops, count, n, po);
+      const double t = plan_ms(ps, cand);
+      if (t < best_ms) {
+        best_ms = t;
+        best = std::move(cand);
+        best_choice = grown ? 100 + k : k;
+      }
+    }
+  }
+  if (pred_ms) *pred_ms = best_ms;
+  if (greedy_ms) *greedy_ms = judge;
+  if (choice) *choice = best_choice;
+  return best;
+}
+
+}  // namespace qcs

@@ -1,0 +1,77 @@
+"""The learned fusion cost model on the GPU.
+
+* its CUDA forward/backward kernels give the FP64 checker's loss and
+  gradients (oracle/mlp.py) to FP32 accuracy;
+* Adam training on the GPU fits a known function;
+* the host copy used for planning predicts what the device predicts;
+* timing collection yields one record per plan item;
+* the learned plan leaves the state equal to the greedy-fused state
+  (infidelity <= 1e-6).
+"""
+import numpy as np
+import pytest
+
+from oracle import mlp
+from oracle import oracle as O
+from qcs_gb300 import capi
+from qcs_gb300 import workloads as W
+from tests.helpers import infidelity
+
+pytestmark = pytest.mark.gpu
+F = capi.COSTMODEL_FEATURES
+
+
+def test_gradients_match_fp64_checker():
+    m = capi.CostModel(seed=3)
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(300, F)).astype(np.float32)  # spans several CTAs (64 rows each)
+    y = rng.normal(size=300).astype(np.float32)
+    loss, g = m.loss_grad(x, y)
+    p = m.params().astype(np.float64)
+    ref_loss, ref_g = mlp.loss_grad(p, x, y, F)
+    assert abs(loss - ref_loss) <= 1e-5 * max(1.0, ref_loss)
+    scale = np.max(np.abs(ref_g))
+    assert np.max(np.abs(g - ref_g)) <= 1e-4 * scale
+    pred = m.predict(x)
+    np.testing.assert_allclose(pred, mlp.forward(p, x, F), rtol=1e-4, atol=1e-4)
+    m.close()
+
+
+def test_training_fits_and_host_matches_device():
+    m = capi.CostModel(seed=5)
+    rng = np.random.default_rng(2)
+    x = rng.random(size=(4000, F)).astype(np.float32)
+    y = (3 * x[:, 7] - 2 * x[:, 8] + x[:, 6] * x[:, 18]).astype(np.float32)
+    l0, _ = m.loss_grad(x, y)
+    l1 = m.train(x, y, epochs=40, batch=256, lr=2e-3)
+    assert l1 < 0.05 * l0
+    np.testing.assert_allclose(m.predict(x[:200], host=True), m.predict(x[:200]),
+                               rtol=1e-4, atol=1e-4)
+    m.close()
+
+
+def test_collect_timings_and_learned_plan_state():
+    n = 20
+    g = W.mixed_circuit(n, 6, 11)
+    with capi.State(n, capi.C64) as s:
+        feats, ms = capi.collect_timings(s, g, kmax=6)
+        assert len(ms) > 5 and np.all(ms > 0)
+        assert np.all(feats[:, :7].sum(1) == 1)
+        # a model trained on these few records still yields a valid plan
+        m = capi.CostModel(seed=7)
+        m.train(feats, np.log2(ms), epochs=50, batch=64, lr=2e-3)
+        plan = capi.plan_learned(g, n, 6, m)
+        assert sorted(plan["order"]) == list(range(len(g)))
+        s.set_basis(0)
+        s.run(g, fusion_k=6)
+        greedy = s.amplitudes()
+        s.set_basis(0)
+        s.set_costmodel(m)
+        s.run(g, fusion_k=6, partitioner=capi.PARTITION_LEARNED)
+        learned = s.amplitudes()
+        s.set_costmodel(None)
+        m.close()
+    assert infidelity(learned, greedy) < 1e-6
+    with O.OracleState(n) as o:
+        o.run(g)
+        assert infidelity(learned, o.amplitudes()) < 1e-6
