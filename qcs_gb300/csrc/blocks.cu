@@ -55,22 +55,36 @@ template <typename C, int K> struct BlockU { C u[K * K]; };
 
 template <typename C, int K>
 __global__ void __launch_bounds__(kBlockThreads)
-    k_block_simt(C *v, const TileGeom g, const BlockU<C, K> U) {
+    k_block_simt(C *v, const __grid_constant__ TileGeom g, const __grid_constant__ BlockU<C, K> U) {
   const int Cn = 1 << g.c;        // columns per tile
   const int stride = Cn + 1;      // smem row stride (elements)
   const int L = 1 << g.nT;        // elements per tile
   extern __shared__ unsigned char smem_raw[];
   C *S = reinterpret_cast<C *>(smem_raw);
+  // The lo/hi tables are indexed per lane; kernel parameters live in the
+  // constant bank, which serialises divergent reads, so they go to shared
+  // memory first.
+  __shared__ i64 goff[128];
+  __shared__ unsigned char acol[256];
   const int tid = threadIdx.x;
+  for (int e = tid; e < 64; e += kBlockThreads) {
+    goff[e] = g.goff_lo[e];
+    goff[64 + e] = g.goff_hi[e];
+    acol[e] = g.a_lo[e];
+    acol[64 + e] = g.a_hi[e];
+    acol[128 + e] = g.col_lo[e];
+    acol[192 + e] = g.col_hi[e];
+  }
+  __syncthreads();
   for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x) {
     i64 base = 0;
     for (int j = 0; j < g.nfree; j++) base |= ((tile >> j) & 1LL) << g.freeq[j];
     // gather (global order, coalesced)
     for (int l = tid; l < L; l += kBlockThreads) {
-      int lo = l & 63, hi = l >> 6;
-      i64 off = g.goff_lo[lo] + g.goff_hi[hi];
-      int a = g.a_lo[lo] + g.a_hi[hi];
-      int col = g.col_lo[lo] + g.col_hi[hi];
+      const int lo = l & 63, hi = l >> 6;
+      const i64 off = goff[lo] + goff[64 + hi];
+      const int a = acol[lo] + acol[64 + hi];
+      const int col = acol[128 + lo] + acol[192 + hi];
       S[a * stride + col] = v[base + off];
     }
     __syncthreads();
@@ -88,10 +102,10 @@ __global__ void __launch_bounds__(kBlockThreads)
     }
     __syncthreads();
     for (int l = tid; l < L; l += kBlockThreads) {
-      int lo = l & 63, hi = l >> 6;
-      i64 off = g.goff_lo[lo] + g.goff_hi[hi];
-      int a = g.a_lo[lo] + g.a_hi[hi];
-      int col = g.col_lo[lo] + g.col_hi[hi];
+      const int lo = l & 63, hi = l >> 6;
+      const i64 off = goff[lo] + goff[64 + hi];
+      const int a = acol[lo] + acol[64 + hi];
+      const int col = acol[128 + lo] + acol[192 + hi];
       v[base + off] = S[a * stride + col];
     }
     __syncthreads();

@@ -69,14 +69,32 @@ __device__ __forceinline__ double na_warp_sum(double x) {
   return x;
 }
 
-// Probability mass of each tile, FP64, into prefix[0..n_tiles).
+// A thread's share of a tile's probability mass, with the same arithmetic
+// as qcs_cuda_sample: FP64 for complex128; for complex64 an FP32 partial over
+// the thread's amplitudes, added in FP64.
+template <typename C>
+__device__ __forceinline__ double na_thread_mass(const C *v, i64 first, i64 tile) {
+  double a = 0.0;
+  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) a += na_prob(v[first + j]);
+  return a;
+}
+template <>
+__device__ __forceinline__ double na_thread_mass<float2>(const float2 *v, i64 first, i64 tile) {
+  float a = 0.f;
+  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) {
+    const float2 x = v[first + j];
+    a = fmaf(x.x, x.x, fmaf(x.y, x.y, a));
+  }
+  return (double)a;
+}
+
+// Probability mass of each tile into prefix[0..n_tiles).
 template <typename C>
 __global__ void __launch_bounds__(256)
     k_na_tile_sums(const C *v, i64 tile, i64 n_tiles, double *prefix) {
   __shared__ double part[8];
   for (i64 t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-    double a = 0.0;
-    for (i64 j = threadIdx.x; j < tile; j += blockDim.x) a += na_prob(v[t * tile + j]);
+    double a = na_thread_mass<C>(v, t * tile, tile);
     a = na_warp_sum(a);
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = a;
     __syncthreads();

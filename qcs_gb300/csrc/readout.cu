@@ -300,13 +300,32 @@ __device__ __forceinline__ double prob64(C x) {
   return ((double)x.x * (double)x.x) + ((double)x.y * (double)x.y);
 }
 
-// Per-tile probability mass, FP64.
+// Per-tile probability mass.  complex128: FP64 throughout.  complex64: each
+// thread sums its amplitudes' |a|^2 in FP32 and adds that partial in FP64
+// (GB300's FP64 rate would otherwise bound this pass); a tile total off by
+// ~1e-7 of itself only moves that much mass onto the tile's last index in
+// k_sample's edge rule.
+template <typename C>
+__device__ __forceinline__ double thread_tile_mass(const C *v, i64 first, i64 tile) {
+  double a = 0.0;
+  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) a += prob64(v[first + j]);
+  return a;
+}
+template <>
+__device__ __forceinline__ double thread_tile_mass<float2>(const float2 *v, i64 first, i64 tile) {
+  float a = 0.f;
+  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) {
+    const float2 x = v[first + j];
+    a = fmaf(x.x, x.x, fmaf(x.y, x.y, a));
+  }
+  return (double)a;
+}
+
 template <typename C>
 __global__ void __launch_bounds__(kReduceThreads)
     k_tile_sums(const C *v, i64 tile, i64 n_tiles, double *sums) {
   for (i64 t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-    double a = 0.0;
-    for (i64 j = threadIdx.x; j < tile; j += blockDim.x) a += prob64(v[t * tile + j]);
+    double a = thread_tile_mass<C>(v, t * tile, tile);
     __shared__ ReduceSlot slot;
     block_sum4(a, 0.0, 0.0, 0.0, &slot);
     __syncthreads();
