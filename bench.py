@@ -552,36 +552,40 @@ def run_random20(args, dist):
 
 
 def run_grover(args, dist):
-    """QFT on a random basis state, a Hadamard layer, then 64 x (phase flip on a
-    random marked index, diffusion), complex64, at --qubits (33 or 34).
-    Reports HBM GB/s per sweep type from per-launch events, and checks argmax
-    and the marked probability against the FP64 oracle at --parity-qubits."""
+    """QFT on a random basis state, then (from |0...0>) a Hadamard layer and
+    64 x (phase flip on a random marked index, diffusion), complex64, at
+    --qubits (33 or 34).  Reports HBM GB/s per sweep type from per-launch
+    events, plain and fused, and checks the Grover part's argmax (the marked
+    index) and marked probability against the FP64 oracle at --parity-qubits."""
     from oracle import oracle as O
     from qcs_gb300 import build as B
     from qcs_gb300 import capi
     from qcs_gb300 import workloads as W
     B.build()
     n = args.qubits
-    basis, marked, g = W.grover_workload(n, args.seed, iterations=64)
-    ops = g.ops()
+    basis, marked, qft, gro = W.grover_workload(n, args.seed, iterations=64)
+    parts = (("qft", basis, qft.ops()), ("grover", 0, gro.ops()))
     res = {}
     with capi.State(n, capi.C64) as s:
         for k, label in ((0, "plain"), (args.fusion_k, "fused")):
-            s.set_basis(basis)
-            s.run(ops, fusion_k=k)  # warm-up
-            s.synchronize()
-            s.set_basis(basis)
-            s.profile(True)
-            e0 = s.event()
-            s.run(ops, fusion_k=k)
-            e1 = s.event()
-            ms = capi.State.elapsed_ms(e0, e1)
-            prof = s.profile_read()
-            s.profile(False)
-            res[label] = {"ms": ms, "ops_per_s": len(g) / (ms / 1e3),
-                          "by_kernel": {c: {"launches": v[0], "ms": v[1],
-                                            "GB/s": v[2] / (v[1] / 1e3) / 1e9}
-                                        for c, v in prof.items()}}
+            row = {}
+            for name, start, ops in parts:
+                s.set_basis(start)
+                s.run(ops, fusion_k=k)  # warm-up
+                s.synchronize()
+                s.set_basis(start)
+                s.profile(True)
+                e0 = s.event()
+                s.run(ops, fusion_k=k)
+                e1 = s.event()
+                ms = capi.State.elapsed_ms(e0, e1)
+                prof = s.profile_read()
+                s.profile(False)
+                row[name] = {"ms": ms, "ops": len(ops), "ops_per_s": len(ops) / (ms / 1e3),
+                             "by_kernel": {c: {"launches": v[0], "ms": v[1],
+                                               "GB/s": v[2] / (v[1] / 1e3) / 1e9}
+                                           for c, v in prof.items()}}
+            res[label] = row
         res["argmax"] = s.argmax()
         res["marked"] = marked
         res["p_marked"] = s.probability(marked)
@@ -589,19 +593,18 @@ def run_grover(args, dist):
     if not args.no_parity:
         O.build()
         pn = cpu_qubits(args.parity_qubits, buffers=1)
-        pb, pm, pg = W.grover_workload(pn, args.seed, iterations=64)
-        full = W.basis_gates(pn, pb)
-        full.extend(pg)
+        _, pm, _, pg = W.grover_workload(pn, args.seed, iterations=64)
         with O.OracleState(pn) as o:
-            o.run(full)
+            o.run(pg)
             oarg, op = o.argmax(), o.probability(pm)
         with capi.State(pn, capi.C64) as s:
-            s.run(full.ops(), fusion_k=args.fusion_k)
+            s.run(pg.ops(), fusion_k=args.fusion_k)
             garg, gp = s.argmax(), s.probability(pm)
-        parity = {"qubits": pn, "argmax_gpu": garg, "argmax_fp64": oarg,
-                  "argmax_equal": garg == oarg, "p_marked_gpu": gp, "p_marked_fp64": op}
-    line = {"mode": "grover", "qubits": n, "state_bytes": 8 << n, "ops": len(g),
-            "results": res, "parity": parity}
+        parity = {"qubits": pn, "marked": pm, "argmax_gpu": garg, "argmax_fp64": oarg,
+                  "argmax_equal": garg == oarg, "p_marked_gpu": gp, "p_marked_fp64": op,
+                  "p_marked_rel_err": abs(gp - op) / op}
+    line = {"mode": "grover", "qubits": n, "state_bytes": 8 << n, "results": res,
+            "parity": parity}
     print(json.dumps(line), flush=True)
 
 

@@ -13,9 +13,9 @@ configurations of this backend:
 * ``brick_circuit``   -- per layer RZ.RY.RZ on every qubit (angles uniform
   in [0, 2 pi)), then CNOT(2i, 2i+1) on even layers and CNOT(2i+1, 2i+2) on
   odd layers.
-* ``grover_workload`` -- random basis state, QFT, a Hadamard layer and then
-  ``iterations`` x (phase flip on a random marked index, diffusion), the
-  structure of ``qc_grover_search`` (src/qcs.c:402-419).
+* ``grover_workload`` -- QFT on a random basis state; separately, a Hadamard
+  layer and ``iterations`` x (phase flip on a random marked index, diffusion)
+  from |0...0>, the structure of ``qc_grover_search`` (src/qcs.c:402-419).
 * ``variational_batch`` -- instances with n ~ U[10, 22] and depth
   ~ U[4, 16]; per layer RY and RZ on every qubit, then a linear CNOT ladder.
 * ``mixed_circuit``   -- per layer a random rotation on every qubit, then
@@ -202,18 +202,27 @@ def brick_circuit(n: int, depth: int, seed: int) -> GateList:
 
 
 def grover_workload(n: int, seed: int, iterations: int = 64):
-    """(basis, marked, gate list) for the QFT + Grover workload."""
+    """(basis, marked, QFT part, Grover part).
+
+    The QFT part is qc_quantum_fourier_transform on the random basis state
+    |basis>.  The Grover part is qc_grover_search's structure on |0...0>: a
+    Hadamard layer, then `iterations` x (phase flip on the random marked
+    index, diffusion), so the marked index dominates (by ~1e4 after 64
+    iterations at 28 qubits).  Run back to back on one state, the Grover part
+    would act on the QFT's output, where no amplitude dominates (the top two
+    probabilities differ by 1e-7 relative at 20 qubits) and an argmax is
+    decided by rounding."""
     rng = Rng(seed)
     basis = rng.below(1 << n)
     marked = rng.below(min(1 << n, 1 << 31))
-    g = GateList()
-    g.extend(qft_gates(n))
+    qft = qft_gates(n)
+    gro = GateList()
     for q in range(n):
-        g.add(H, q)
+        gro.add(H, q)
     for _ in range(iterations):
-        g.add(PHASE_FLIP, index=marked)
-        g.add(DIFFUSION)
-    return basis, marked, g
+        gro.add(PHASE_FLIP, index=marked)
+        gro.add(DIFFUSION)
+    return basis, marked, qft, gro
 
 
 def variational_instance(rng: Rng, n_range=(10, 22), depth_range=(4, 16)):

@@ -242,8 +242,9 @@ def test_grover_physical(prec, golden):
         np.testing.assert_allclose(s.amplitudes(), d["physical"], atol=1e-6)
         assert s.argmax() == 42
     n = 12
-    basis, marked, g = W.grover_workload(n, 4, iterations=20)
+    basis, marked, qft, g = W.grover_workload(n, 4, iterations=20)
     full = W.basis_gates(n, basis)
+    full.extend(qft)
     full.extend(g)
     with capi.State(n, prec) as s, oracle_state(n, full) as o:
         s.run(full)
@@ -362,8 +363,9 @@ def test_fused_circuit_tensor_cores(k):
 
 def test_fused_with_grover_barriers():
     n = 11
-    basis, marked, g = W.grover_workload(n, 6, iterations=8)
+    basis, marked, qft, g = W.grover_workload(n, 6, iterations=8)
     full = W.basis_gates(n, basis)
+    full.extend(qft)
     full.extend(g)
     with capi.State(n, capi.C64) as s, oracle_state(n, full) as o:
         s.run(full, fusion_k=4)
