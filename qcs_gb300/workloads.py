@@ -13,9 +13,9 @@ configurations of this backend:
 * ``brick_circuit``   -- per layer RZ.RY.RZ on every qubit (angles uniform
   in [0, 2 pi)), then CNOT(2i, 2i+1) on even layers and CNOT(2i+1, 2i+2) on
   odd layers.
-* ``grover_workload`` -- QFT on a random basis state; separately, a Hadamard
-  layer and ``iterations`` x (phase flip on a random marked index, diffusion)
-  from |0...0>, the structure of ``qc_grover_search`` (src/qcs.c:402-419).
+* ``grover_workload`` -- QFT on a random basis state, then rounds of
+  (Hadamard layer, phase flip on a random marked index, diffusion); and the
+  structure of ``qc_grover_search`` (src/qcs.c:402-419) from |0...0>.
 * ``variational_batch`` -- instances with n ~ U[10, 22] and depth
   ~ U[4, 16]; per layer RY and RZ on every qubit, then a linear CNOT ladder.
 * ``mixed_circuit``   -- per layer a random rotation on every qubit, then
@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
+from typing import NamedTuple
 
 import numpy as np
 
@@ -201,28 +202,40 @@ def brick_circuit(n: int, depth: int, seed: int) -> GateList:
     return g
 
 
-def grover_workload(n: int, seed: int, iterations: int = 64):
-    """(basis, marked, QFT part, Grover part).
+class GroverWorkload(NamedTuple):
+    basis: int       # start of the QFT part
+    marked: int      # the phase-flipped index
+    qft: GateList    # qc_quantum_fourier_transform
+    rounds: GateList  # iterations x (Hadamard layer, phase flip, diffusion)
+    search: GateList  # Hadamard layer, then iterations x (phase flip, diffusion)
 
-    The QFT part is qc_quantum_fourier_transform on the random basis state
-    |basis>.  The Grover part is qc_grover_search's structure on |0...0>: a
-    Hadamard layer, then `iterations` x (phase flip on the random marked
-    index, diffusion), so the marked index dominates (by ~1e4 after 64
-    iterations at 28 qubits).  Run back to back on one state, the Grover part
-    would act on the QFT's output, where no amplitude dominates (the top two
-    probabilities differ by 1e-7 relative at 20 qubits) and an argmax is
-    decided by rounding."""
+
+def grover_workload(n: int, seed: int, iterations: int = 64) -> GroverWorkload:
+    """The 33/34-qubit workload: QFT on the random basis state |basis>, then
+    `iterations` rounds of (Hadamard layer, phase flip on the random marked
+    index, diffusion) -- `qft` followed by `rounds`.
+
+    After those rounds no amplitude dominates: at 16 qubits the top
+    probabilities agree to 4e-16 relative, so which index is the argmax is
+    decided by rounding, in FP64 too.  `search` is qc_grover_search's own
+    structure (src/qcs.c:402-419) with the same marked index and iteration
+    count, run from |0...0>: one Hadamard layer, then `iterations` x (phase
+    flip, diffusion).  There the marked index dominates (by ~1e4 at 28
+    qubits), so its argmax is a well-posed basis-state answer."""
     rng = Rng(seed)
     basis = rng.below(1 << n)
     marked = rng.below(min(1 << n, 1 << 31))
-    qft = qft_gates(n)
-    gro = GateList()
+    rounds = GateList()
+    search = GateList()
     for q in range(n):
-        gro.add(H, q)
+        search.add(H, q)
     for _ in range(iterations):
-        gro.add(PHASE_FLIP, index=marked)
-        gro.add(DIFFUSION)
-    return basis, marked, qft, gro
+        for q in range(n):
+            rounds.add(H, q)
+        for g in (rounds, search):
+            g.add(PHASE_FLIP, index=marked)
+            g.add(DIFFUSION)
+    return GroverWorkload(basis, marked, qft_gates(n), rounds, search)
 
 
 def variational_instance(rng: Rng, n_range=(10, 22), depth_range=(4, 16)):

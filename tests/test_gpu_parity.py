@@ -242,14 +242,19 @@ def test_grover_physical(prec, golden):
         np.testing.assert_allclose(s.amplitudes(), d["physical"], atol=1e-6)
         assert s.argmax() == 42
     n = 12
-    basis, marked, qft, g = W.grover_workload(n, 4, iterations=20)
-    full = W.basis_gates(n, basis)
-    full.extend(qft)
-    full.extend(g)
+    w = W.grover_workload(n, 4, iterations=20)
+    with capi.State(n, prec) as s, oracle_state(n, w.search) as o:
+        s.run(w.search)
+        assert s.argmax() == o.argmax() == w.marked
+        assert abs(s.probability(w.marked) - o.probability(w.marked)) < 1e-5
+    full = W.basis_gates(n, w.basis)
+    full.extend(w.qft)
+    full.extend(w.rounds)
     with capi.State(n, prec) as s, oracle_state(n, full) as o:
         s.run(full)
-        assert s.argmax() == o.argmax()
-        assert abs(s.probability(marked) - o.probability(marked)) < 1e-5
+        assert infidelity(s.amplitudes(), o.amplitudes()) < 1e-8
+        pm = o.probability(w.marked)
+        assert abs(s.probability(w.marked) - pm) < 1e-4 * pm
 
 
 # ---- fused blocks ---------------------------------------------------------------------
@@ -363,14 +368,16 @@ def test_fused_circuit_tensor_cores(k):
 
 def test_fused_with_grover_barriers():
     n = 11
-    basis, marked, qft, g = W.grover_workload(n, 6, iterations=8)
-    full = W.basis_gates(n, basis)
-    full.extend(qft)
-    full.extend(g)
+    w = W.grover_workload(n, 6, iterations=8)
+    full = W.basis_gates(n, w.basis)
+    full.extend(w.qft)
+    full.extend(w.rounds)
     with capi.State(n, capi.C64) as s, oracle_state(n, full) as o:
         s.run(full, fusion_k=4)
-        assert s.argmax() == o.argmax()
         assert infidelity(s.amplitudes(), o.amplitudes()) < C64_INFID
+    with capi.State(n, capi.C64) as s, oracle_state(n, w.search) as o:
+        s.run(w.search, fusion_k=4)
+        assert s.argmax() == o.argmax() == w.marked
 
 
 # ---- full size: size-independent properties ------------------------------------------

@@ -92,9 +92,9 @@ def test_plan_is_a_valid_reordering(kmax):
 
 def test_plan_keeps_non_gate_ops_as_barriers():
     n = 6
-    basis, marked, qft, g = W.grover_workload(n, 3, iterations=3)
-    qft.extend(g)
-    g = qft
+    w = W.grover_workload(n, 3, iterations=3)
+    g = w.qft
+    g.extend(w.rounds)
     order, item, nitems = capi.plan(g, n, 4)
     kinds = g.ops()["kind"][order]
     flips = np.nonzero(kinds == W.PHASE_FLIP)[0]
