@@ -87,8 +87,15 @@ typedef struct qcs_cuda_run_options {
                     dense blocks of at most fusion_k qubits               */
   int fusion_engine; /* QCS_FUSE_AUTO, QCS_FUSE_SIMT or QCS_FUSE_TENSOR    */
   int partitioner;   /* QCS_PARTITION_GREEDY or QCS_PARTITION_LEARNED     */
-  int reserved;
+  int flags;         /* QCS_RUN_* bits, 0 by default                      */
 } qcs_cuda_run_options;
+
+/* A fused run keeps its plan and block matrices with the state, keyed on the
+ * exact bytes of the op list and on the options (and, for the learned
+ * partitioner, the cost model and its current parameters); running the same
+ * list again skips planning.  Any change (one angle) plans afresh.  This bit
+ * plans afresh every time and leaves the kept plan untouched. */
+#define QCS_RUN_NO_PLAN_CACHE 1
 
 #define QCS_FUSE_AUTO 0
 #define QCS_FUSE_SIMT 1   /* FP32 CUDA-core block kernel (k <= 5)          */
@@ -282,7 +289,9 @@ int qcs_cuda_state_set_costmodel(qcs_cuda_state *s, qcs_cuda_costmodel *m);
 /* Host only: the learned plan for a num_qubits state (order/item as in
  * qcs_cuda_plan), the model's predicted ms for it and for the greedy
  * width-kmax plan, and which candidate won (2..7: greedy width; 100 + k:
- * model-stopped growth at width k). */
+ * model-stopped growth at width k), plus 1000 x the number of that
+ * candidate's blocks the model then split into narrower items or widened
+ * onto the tensor cores. */
 int qcs_cuda_plan_learned(const qcs_cuda_op *ops, int count, int num_qubits,
                           int kmax, qcs_cuda_costmodel *m, int *order,
                           int *item, int *num_items, double *pred_ms,

@@ -39,9 +39,12 @@ class QcsCudaError(RuntimeError):
         self.status = status
 
 
+RUN_NO_PLAN_CACHE = 1
+
+
 class RunOptions(C.Structure):
     _fields_ = [("fusion_k", C.c_int), ("fusion_engine", C.c_int),
-                ("partitioner", C.c_int), ("reserved", C.c_int)]
+                ("partitioner", C.c_int), ("flags", C.c_int)]
 
 
 _lib = None
@@ -243,10 +246,10 @@ class State:
         _check(lib().qcs_cuda_diffusion(self._h))
 
     def run(self, gates, fusion_k: int = 0, engine: int = FUSE_AUTO,
-            partitioner: int = PARTITION_GREEDY):
+            partitioner: int = PARTITION_GREEDY, plan_cache: bool = True):
         ops = gates.ops() if isinstance(gates, W.GateList) else np.ascontiguousarray(gates)
         assert ops.dtype == W.OP_DTYPE
-        opt = RunOptions(fusion_k, engine, partitioner, 0)
+        opt = RunOptions(fusion_k, engine, partitioner, 0 if plan_cache else RUN_NO_PLAN_CACHE)
         _check(lib().qcs_cuda_run(self._h, ops.ctypes.data_as(C.c_void_p), len(ops),
                                   C.byref(opt)))
 

@@ -239,11 +239,59 @@ static int apply_op(qcs_cuda_state *s, const qcs_cuda_op &o) {
   return apply_1q(s, m, o.target);
 }
 
+static int apply_block_item(qcs_cuda_state *s, const PlanItem &it, int engine,
+                            const std::vector<cd> &u);
+
 static int apply_item(qcs_cuda_state *s, const qcs_cuda_op *ops, const PlanItem &it, int engine,
                       std::vector<cd> &u) {
   if (it.kind == 1) return apply_op(s, ops[it.op]);
   if (it.gates.size() == 1) return apply_op(s, ops[it.gates[0]]);
   block_matrix(ops, it, u);
+  return apply_block_item(s, it, engine, u);
+}
+
+static int fusion_cap(const qcs_cuda_state *s, int k, int engine) {
+  int kcap = (engine != QCS_FUSE_SIMT && tc_supported(s, 6)) ? 6 : kSimtMaxK;
+  if (k > kcap) k = kcap;
+  if (k > s->n) k = s->n;
+  return k;
+}
+
+// The plan of the last fused run, with its block matrices, kept per state:
+// circuits are usually run many times over (shots in separate runs, sweeps
+// of the same circuit, benchmarks), and planning -- above all the learned
+// partitioner, which scores many candidate plans with the MLP -- costs host
+// time before the first kernel can start.  The key is the exact op bytes
+// plus everything the plan depends on.
+struct PlanCache {
+  std::vector<qcs_cuda_op> ops;
+  int n = -1, k = 0, engine = 0, partitioner = 0;
+  const qcs_cuda_costmodel *cm = nullptr;
+  unsigned long long cm_gen = 0;
+  std::vector<PlanItem> plan;
+  std::vector<std::vector<cd>> mats;  // per item: the block matrix, or empty
+};
+
+// Block matrices are kept while their total stays under this many bytes.
+constexpr size_t kPlanCacheMatBytes = 64u << 20;
+
+void plan_cache_free(qcs_cuda_state *s) {
+  delete s->plans;
+  s->plans = nullptr;
+}
+
+static bool plan_cache_hit(const PlanCache *c, const qcs_cuda_op *ops, int count, int n, int k,
+                           int engine, int partitioner, const qcs_cuda_costmodel *cm,
+                           unsigned long long gen) {
+  return c && c->n == n && c->k == k && c->engine == engine && c->partitioner == partitioner &&
+         c->cm == cm && c->cm_gen == gen && (int)c->ops.size() == count &&
+         (count == 0 || memcmp(c->ops.data(), ops, (size_t)count * sizeof(qcs_cuda_op)) == 0);
+}
+
+static bool item_is_block(const PlanItem &it) { return it.kind == 0 && it.gates.size() > 1; }
+
+static int apply_block_item(qcs_cuda_state *s, const PlanItem &it, int engine,
+                            const std::vector<cd> &u) {
   const int kb = (int)it.qubits.size();
   if (kb == 1) {
     double m[8] = {u[0].real(), u[0].imag(), u[1].real(), u[1].imag(),
@@ -252,13 +300,6 @@ static int apply_item(qcs_cuda_state *s, const qcs_cuda_op *ops, const PlanItem 
   }
   return apply_block(s, kb, it.qubits.data(), reinterpret_cast<const double *>(u.data()), engine,
                      false);
-}
-
-static int fusion_cap(const qcs_cuda_state *s, int k, int engine) {
-  int kcap = (engine != QCS_FUSE_SIMT && tc_supported(s, 6)) ? 6 : kSimtMaxK;
-  if (k > kcap) k = kcap;
-  if (k > s->n) k = s->n;
-  return k;
 }
 
 int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda_run_options *opt) {
@@ -274,8 +315,24 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
   }
   const int engine = opt->fusion_engine;
   k = fusion_cap(s, k, engine);
+  const bool learned = opt->partitioner == QCS_PARTITION_LEARNED && costmodel_ready(s->cm);
+  const int part = learned ? QCS_PARTITION_LEARNED : QCS_PARTITION_GREEDY;
+  const qcs_cuda_costmodel *cm = learned ? s->cm : nullptr;
+  const unsigned long long gen = learned ? costmodel_generation(s->cm) : 0;
+  const bool use_cache = !(opt->flags & QCS_RUN_NO_PLAN_CACHE);
+  if (use_cache && plan_cache_hit(s->plans, ops, count, s->n, k, engine, part, cm, gen)) {
+    const PlanCache &c = *s->plans;
+    std::vector<cd> u;
+    for (size_t i = 0; i < c.plan.size(); i++) {
+      const PlanItem &it = c.plan[i];
+      rc = (item_is_block(it) && !c.mats[i].empty()) ? apply_block_item(s, it, engine, c.mats[i])
+                                                     : apply_item(s, ops, it, engine, u);
+      if (rc) return rc;
+    }
+    return QCS_CUDA_OK;
+  }
   std::vector<PlanItem> plan;
-  if (opt->partitioner == QCS_PARTITION_LEARNED && costmodel_ready(s->cm)) {
+  if (learned) {
     const bool simt_only = engine == QCS_FUSE_SIMT;
     plan = partition_learned(ops, count, s->n, k, s->cm, !simt_only && tc_supported(s, 5),
                              !simt_only && tc_supported(s, 6), nullptr, nullptr, nullptr);
@@ -286,10 +343,39 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
     po.cost_ctx = nullptr;
     plan = partition(ops, count, s->n, po);
   }
+  PlanCache *c = nullptr;
+  if (use_cache) {
+    if (!s->plans) s->plans = new PlanCache();
+    c = s->plans;
+    c->n = -1;  // invalid until the run completes
+    c->ops.assign(ops, ops + count);
+    c->mats.assign(plan.size(), std::vector<cd>());
+  }
+  size_t kept = 0;
   std::vector<cd> u;
-  for (const PlanItem &it : plan) {
-    rc = apply_item(s, ops, it, engine, u);
+  for (size_t i = 0; i < plan.size(); i++) {
+    const PlanItem &it = plan[i];
+    if (!item_is_block(it)) {
+      rc = apply_item(s, ops, it, engine, u);
+    } else {
+      block_matrix(ops, it, u);
+      rc = apply_block_item(s, it, engine, u);
+      const size_t bytes = u.size() * sizeof(cd);
+      if (c && kept + bytes <= kPlanCacheMatBytes) {
+        c->mats[i] = u;
+        kept += bytes;
+      }
+    }
     if (rc) return rc;
+  }
+  if (c) {
+    c->plan = std::move(plan);
+    c->n = s->n;
+    c->k = k;
+    c->engine = engine;
+    c->partitioner = part;
+    c->cm = cm;
+    c->cm_gen = gen;
   }
   return QCS_CUDA_OK;
 }
@@ -311,13 +397,17 @@ int collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, int km
   std::vector<cd> u;
   for (size_t i = 0; i < plan.size(); i++) {
     const bool timed = plan[i].kind == 0 && (int)rec.size() < max;
+    // the block matrix is formed before the opening event: host work while
+    // the stream waits must not count as the kernel's time
+    const bool block = item_is_block(plan[i]);
+    if (block) block_matrix(ops, plan[i], u);
     cudaEvent_t a = nullptr, b = nullptr;
     if (timed) {
       cudaEventCreate(&a);
       cudaEventCreate(&b);
       cudaEventRecord(a, s->stream);
     }
-    rc = apply_item(s, ops, plan[i], engine, u);
+    rc = block ? apply_block_item(s, plan[i], engine, u) : apply_item(s, ops, plan[i], engine, u);
     if (timed) {
       cudaEventRecord(b, s->stream);
       ev.push_back(a);

@@ -51,6 +51,8 @@ enum KClass {
 
 struct ProfData;  // per-state event bookkeeping (state.cu)
 struct TcRing;    // tensor-core engine block-matrix uploads (blocks_tc.cu)
+struct PlanCache; // kept fused plan of the last run (blocks.cu)
+void plan_cache_free(qcs_cuda_state *s);
 void tc_release(TcRing *r);
 
 }  // namespace qcs
@@ -85,6 +87,7 @@ struct qcs_cuda_state {
   qcs::TcRing *tc;        // created on first tensor-core block
   int *d_err;             // device error flag (bounded waits that gave up)
   qcs_cuda_costmodel *cm; // model for QCS_PARTITION_LEARNED (not owned)
+  qcs::PlanCache *plans;  // last fused run's plan and block matrices
 };
 
 namespace qcs {

@@ -109,6 +109,62 @@ static double grow_cost(int n, int k, int ngates, const int *qubits, void *ctx) 
   return exp2((double)costmodel_predict_host(ps.m, f));
 }
 
+// Cheapest predicted way to run one block's gates: the block itself, its
+// gates re-partitioned greedily at every narrower width (width 1: every gate
+// on its own, or merged with same-qubit neighbours), or the block widened to
+// five qubits for the tensor cores.  The block's gate order is a valid execution order of those
+// gates, so each alternative may replace the block in place.  Returns true
+// (and fills *out) when an alternative is predicted faster.
+static bool refine_block(const PlanScore &ps, const PlanItem &it, std::vector<PlanItem> *out) {
+  const int m = (int)it.gates.size();
+  const int k = (int)it.qubits.size();
+  if (it.kind != 0 || m < 2 || k < 2) return false;
+  std::vector<qcs_cuda_op> sub(m);
+  for (int j = 0; j < m; j++) sub[j] = ps.ops[it.gates[j]];
+  PlanScore sps = ps;
+  sps.ops = sub.data();
+  const double t_block = item_ms(sps, [&] {
+    PlanItem local = it;
+    for (int j = 0; j < m; j++) local.gates[j] = j;
+    return local;
+  }());
+  double best = t_block;
+  std::vector<PlanItem> best_items;
+  for (int kk = 1; kk < k; kk++) {
+    PartitionOptions po;
+    po.kmax = kk;
+    po.cost = nullptr;
+    po.cost_ctx = nullptr;
+    std::vector<PlanItem> cand = partition(sub.data(), m, ps.n, po);
+    const double t = plan_ms(sps, cand);
+    if (t < best) {
+      best = t;
+      best_items = std::move(cand);
+    }
+  }
+  // Widened onto the tensor cores: a block of k < 5 qubits padded with the
+  // lowest qubits it does not touch (identity there) runs as a 5-qubit
+  // tensor-core block instead of a CUDA-core one.
+  if (ps.tc5 && k < 5 && ps.n >= 5) {
+    PlanItem wide = it;
+    for (int j = 0; j < m; j++) wide.gates[j] = j;
+    for (int q = 0; q < ps.n && (int)wide.qubits.size() < 5; q++)
+      if (std::find(it.qubits.begin(), it.qubits.end(), q) == it.qubits.end())
+        wide.qubits.push_back(q);
+    std::sort(wide.qubits.begin(), wide.qubits.end());
+    const double t = item_ms(sps, wide);
+    if (t < best) {
+      best = t;
+      best_items.assign(1, std::move(wide));
+    }
+  }
+  if (best_items.empty()) return false;
+  for (PlanItem &x : best_items)
+    for (int &g : x.gates) g = it.gates[g];
+  *out = std::move(best_items);
+  return true;
+}
+
 std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n, int kmax,
                                         const qcs_cuda_costmodel *m, bool tc_ok_5,
                                         bool tc_ok_6, double *pred_ms, double *greedy_ms,
@@ -138,9 +194,28 @@ std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n
       }
     }
   }
+  // Block by block: split the blocks the model predicts slower than their
+  // parts (a wide block holding a few diagonal gates, say), or widen the
+  // narrow ones it predicts faster on the tensor cores.
+  std::vector<PlanItem> refined;
+  refined.reserve(best.size());
+  int splits = 0;
+  for (PlanItem &it : best) {
+    std::vector<PlanItem> parts;
+    if (refine_block(ps, it, &parts)) {
+      for (PlanItem &x : parts) refined.push_back(std::move(x));
+      splits++;
+    } else {
+      refined.push_back(std::move(it));
+    }
+  }
+  if (splits) {
+    best = std::move(refined);
+    best_ms = plan_ms(ps, best);
+  }
   if (pred_ms) *pred_ms = best_ms;
   if (greedy_ms) *greedy_ms = judge;
-  if (choice) *choice = best_choice;
+  if (choice) *choice = best_choice + 1000 * splits;
   return best;
 }
 

@@ -43,6 +43,8 @@ std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n
 
 float costmodel_predict_host(const struct ::qcs_cuda_costmodel *m, const float *x);
 bool costmodel_ready(const struct ::qcs_cuda_costmodel *m);
+// Changes whenever the model's parameters change (training, set_params).
+unsigned long long costmodel_generation(const struct ::qcs_cuda_costmodel *m);
 int costmodel_features(const struct ::qcs_cuda_costmodel *m);
 
 }  // namespace qcs

@@ -9,6 +9,7 @@
 // slots in a fixed order, so gradients are deterministic.  There is nothing
 // like it in the reference (its only optimisation is the gate-history
 // peephole of qc_optimize, src/qcs.c:650-698).
+#include <atomic>
 #include <math.h>
 #include <string.h>
 
@@ -186,6 +187,7 @@ struct qcs_cuda_costmodel {
   int cap_rows;
   int step;
   std::vector<float> host_params;  // mirror for planning on the host
+  unsigned long long generation;   // bumped whenever host_params change
   cudaStream_t stream;
 };
 
@@ -226,7 +228,12 @@ static int cm_grad_device(qcs_cuda_costmodel *m, const float *x, const float *y,
   return check_launch("cost model gradient sum");
 }
 
+// Generations are unique across models, so a plan kept for a destroyed model
+// never matches a new model that happens to reuse its address.
+static std::atomic<unsigned long long> g_cm_generation{0};
+
 static int cm_sync_host(qcs_cuda_costmodel *m) {
+  m->generation = ++g_cm_generation;
   m->host_params.resize(m->count);
   int rc = check_cuda(cudaMemcpyAsync(m->host_params.data(), m->d_params, m->count * sizeof(float),
                                       cudaMemcpyDeviceToHost, m->stream),
@@ -234,29 +241,38 @@ static int cm_sync_host(qcs_cuda_costmodel *m) {
   return rc ? rc : check_cuda(cudaStreamSynchronize(m->stream), "cost model sync");
 }
 
-// Host forward pass (used while planning), FP32 like the device.
+// Host forward pass (used while planning), FP32 like the device: every
+// output sums its inputs in index order, as the row-major loops below do
+// with the input index outermost.
 float costmodel_predict_host(const qcs_cuda_costmodel *m, const float *x) {
   const MlpShape S(m->F);
   const float *w = m->host_params.data();
   float h[kMlpHidden], t[kMlpHidden];
-  for (int j = 0; j < kMlpHidden; j++) {
-    float acc = w[S.off_b1 + j];
-    for (int i = 0; i < m->F; i++) acc += x[i] * w[S.off_w1 + i * kMlpHidden + j];
-    h[j] = acc > 0.f ? acc : 0.f;
+  memcpy(h, w + S.off_b1, sizeof(h));
+  for (int i = 0; i < m->F; i++) {
+    const float xi = x[i];
+    if (xi == 0.f) continue;  // one-hot and flag features are mostly zero
+    const float *row = w + S.off_w1 + i * kMlpHidden;
+    for (int j = 0; j < kMlpHidden; j++) h[j] += xi * row[j];
   }
+  for (int j = 0; j < kMlpHidden; j++) h[j] = h[j] > 0.f ? h[j] : 0.f;
   const int wo[2] = {S.off_w2, S.off_w3}, bo[2] = {S.off_b2, S.off_b3};
   for (int L = 0; L < 2; L++) {
-    for (int j = 0; j < kMlpHidden; j++) {
-      float acc = w[bo[L] + j];
-      for (int i = 0; i < kMlpHidden; i++) acc += h[i] * w[wo[L] + i * kMlpHidden + j];
-      t[j] = acc > 0.f ? acc : 0.f;
+    memcpy(t, w + bo[L], sizeof(t));
+    for (int i = 0; i < kMlpHidden; i++) {
+      const float hi = h[i];
+      if (hi == 0.f) continue;  // ReLU zeros
+      const float *row = w + wo[L] + i * kMlpHidden;
+      for (int j = 0; j < kMlpHidden; j++) t[j] += hi * row[j];
     }
-    memcpy(h, t, sizeof(h));
+    for (int j = 0; j < kMlpHidden; j++) h[j] = t[j] > 0.f ? t[j] : 0.f;
   }
   float o = w[S.off_b4];
   for (int i = 0; i < kMlpHidden; i++) o += h[i] * w[S.off_w4 + i];
   return o;
 }
+
+unsigned long long costmodel_generation(const qcs_cuda_costmodel *m) { return m->generation; }
 
 bool costmodel_ready(const qcs_cuda_costmodel *m) { return m && !m->host_params.empty(); }
 int costmodel_features(const qcs_cuda_costmodel *m) { return m->F; }

@@ -188,6 +188,7 @@ static void free_state(qcs_cuda_state *s) {
   if (!s) return;
   if (s->stream) cudaStreamSynchronize(s->stream);
   prof_free(s);
+  plan_cache_free(s);
   tc_release(s->tc);
   cudaFree(s->d_err);
   cudaFree(s->vec);

@@ -164,7 +164,7 @@ void qc_flush(t_q_circuit *c) {
   opt.fusion_k = c->fusion_k;
   opt.fusion_engine = QCS_FUSE_AUTO;
   opt.partitioner = QCS_PARTITION_GREEDY;
-  opt.reserved = 0;
+  opt.flags = 0;
   rc = qcs_cuda_run(c->state, c->pending, c->num_pending, &opt);
   c->num_pending = 0;
   if (rc != QCS_CUDA_OK)

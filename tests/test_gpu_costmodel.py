@@ -6,7 +6,9 @@
 * the host copy used for planning predicts what the device predicts;
 * timing collection yields one record per plan item;
 * the learned plan leaves the state equal to the greedy-fused state
-  (infidelity <= 1e-6).
+  (infidelity <= 1e-6);
+* a model trained on the simulator's own timings is timed against the
+  greedy plan it is judged by (the gain is recorded with the test).
 """
 import numpy as np
 import pytest
@@ -75,3 +77,68 @@ def test_collect_timings_and_learned_plan_state():
     with O.OracleState(n) as o:
         o.run(g)
         assert infidelity(learned, o.amplitudes()) < 1e-6
+
+
+def _timed_ms(s, g, k, part, reps=5):
+    import statistics
+    s.set_basis(0)
+    s.run(g, fusion_k=k, partitioner=part)  # warm-up; plans and keeps the plan
+    ts = []
+    for _ in range(reps):
+        s.set_basis(0)
+        e0 = s.event()
+        s.run(g, fusion_k=k, partitioner=part)
+        e1 = s.event()
+        ts.append(capi.State.elapsed_ms(e0, e1))
+    return statistics.median(ts)
+
+
+def test_learned_partition_gain_over_greedy(record_property):
+    """What the trained network gains over the method without it: a model
+    trained on this simulator's own timings of random 20-24-qubit circuits
+    plans an unseen 24-qubit mixed circuit; its plan is timed against the
+    greedy width-6 plan (the judge) on the same state.  The learned plan must
+    not be slower beyond timing noise, and must leave the state equal to the
+    greedy-fused one; the measured gain is recorded with the test."""
+    rng = np.random.default_rng(21)
+    feats, times = [], []
+    for n in (20, 22, 24):
+        with capi.State(n, capi.C64) as s:
+            for rep in range(10):
+                seed = int(rng.integers(1 << 30))
+                depth = int(rng.integers(2, 7))
+                g = (W.mixed_circuit(n, depth, seed) if rep % 3 == 0 else
+                     W.brick_circuit(n, depth, seed) if rep % 3 == 1 else
+                     W.random_circuit(n, seed, 40 * depth, with_qft=False)[1])
+                for k in range(1, 7):
+                    eng = capi.FUSE_SIMT if k <= 5 and rep % 2 else capi.FUSE_AUTO
+                    f, ms = capi.collect_timings(s, g, kmax=k, engine=eng)
+                    feats.append(f)
+                    times.append(ms)
+    x = np.concatenate(feats)
+    y = np.log2(np.maximum(np.concatenate(times), 1e-4)).astype(np.float32)
+    m = capi.CostModel(seed=9)
+    m.train(x, y, epochs=60, batch=256, lr=2e-3)
+    n = 24
+    g = W.mixed_circuit(n, 30, 4242)
+    plan = capi.plan_learned(g, n, 6, m)
+    assert plan["pred_ms"] <= plan["greedy_pred_ms"]
+    with capi.State(n, capi.C64) as s:
+        s.set_costmodel(m)
+        t_greedy = _timed_ms(s, g, 6, capi.PARTITION_GREEDY)
+        greedy = s.amplitudes()
+        t_learned = _timed_ms(s, g, 6, capi.PARTITION_LEARNED)
+        learned = s.amplitudes()
+        t_greedy2 = _timed_ms(s, g, 6, capi.PARTITION_GREEDY)
+        s.set_costmodel(None)
+    m.close()
+    t_greedy = min(t_greedy, t_greedy2)
+    gain = t_greedy / t_learned
+    record_property("greedy_ms", t_greedy)
+    record_property("learned_ms", t_learned)
+    record_property("gain", gain)
+    record_property("choice", plan["choice"])
+    print(f"learned {t_learned:.3f} ms greedy {t_greedy:.3f} ms gain {gain:.3f} "
+          f"choice {plan['choice']} records {len(y)}")
+    assert infidelity(learned, greedy) < 1e-6
+    assert gain > 0.9

@@ -380,6 +380,32 @@ def test_fused_with_grover_barriers():
         assert s.argmax() == o.argmax() == w.marked
 
 
+@pytest.mark.parametrize("engine,k", [(capi.FUSE_SIMT, 5), (capi.FUSE_TENSOR, 6)])
+def test_kept_plan_replays_identically(engine, k):
+    """A second run of the same op list reuses the kept plan and block
+    matrices and gives the same amplitudes, bit for bit, as planning afresh;
+    a list with one angle changed is planned afresh."""
+    n = 16
+    g = W.mixed_circuit(n, 12, 5)
+    with capi.State(n, capi.C64) as s:
+        s.run(g, fusion_k=k, engine=engine, plan_cache=False)
+        a = s.amplitudes()
+        for _ in range(2):
+            s.set_basis(0)
+            s.run(g, fusion_k=k, engine=engine)
+            assert np.array_equal(s.amplitudes(), a)
+        ops = g.ops().copy()
+        i = int(np.nonzero(np.isin(ops["kind"], (W.RX, W.RY, W.RZ, W.P)))[0][0])
+        ops["angle"][i] += 0.5
+        s.set_basis(0)
+        s.run(ops, fusion_k=k, engine=engine)
+        c = s.amplitudes()
+        s.set_basis(0)
+        s.run(ops, fusion_k=k, engine=engine, plan_cache=False)
+        assert np.array_equal(s.amplitudes(), c)
+        assert not np.array_equal(a, c)
+
+
 # ---- full size: size-independent properties ------------------------------------------
 
 def _inverse(g: W.GateList) -> W.GateList:
