@@ -435,6 +435,12 @@ def run_ours(args, dist):
 
 SWEEPS = ("dense1q", "diag1q", "phase_mask", "ctrl1q", "cphase", "block_simt4",
           "block_tc6", "block_tc5", "norm", "argmax", "diffuse", "measure", "sample")
+# tensor-core blocks on fixed qubit sets (not in the default list)
+TC_PLACEMENTS = {"block_tc6_low": lambda n: list(range(6)),
+                 "block_tc6_q0": lambda n: [0, 5, 10, 15, 20, 25],
+                 "block_tc6_mid": lambda n: list(range(6, 12)),
+                 "block_tc6_high": lambda n: list(range(n - 6, n)),
+                 "block_tc6_spread": lambda n: [1, 6, 11, 16, 21, 26]}
 
 
 def run_sweeps(args, dist):
@@ -472,6 +478,8 @@ def run_sweeps(args, dist):
                                                   capi.FUSE_TENSOR), 2 * Ns),
             "block_tc5": (lambda i: s.apply_block([(i + 3 * j) % n for j in range(5)], u5,
                                                   capi.FUSE_TENSOR), 2 * Ns),
+            **{name: ((lambda i, q=place(n): s.apply_block(q, u6, capi.FUSE_TENSOR)), 2 * Ns)
+               for name, place in TC_PLACEMENTS.items()},
             "norm": (lambda i: s.norm_sq(), Ns),
             "argmax": (lambda i: s.argmax(), Ns),
             "diffuse": (lambda i: s.diffusion(), 2 * Ns),

@@ -44,6 +44,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
@@ -219,18 +220,12 @@ __device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
   return b;
 }
 
-template <int KA, bool COL_FAST>
-__device__ __forceinline__ void unit_coords(int u, int &m, int &j) {
-  if (COL_FAST) {  // consecutive threads walk consecutive columns (qubit 0 is a column bit)
-    m = u & (kTcM - 1);
-    j = u >> 7;
-  } else {         // consecutive threads walk a column's amplitudes (qubit 0 in the block)
-    j = u & (KA / 4 - 1);
-    m = u / (KA / 4);
-  }
-}
-
-template <int KA, bool COL_FAST>
+// PAIR: qubit 0 is block bit 0, so block rows 2b and 2b+1 of a column are
+// adjacent amplitudes and move as one 16-byte access.  Otherwise qubit 0 is
+// column bit 0 and a warp's 32 columns are (mostly) adjacent amplitudes.
+// Either way a producer thread keeps one column (tile row m = p % 128) and
+// consecutive threads take consecutive columns.
+template <int KA, bool PAIR>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_block_tc(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
                int *err) {
@@ -291,14 +286,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
       const int stage = it & 1;
       const i64 base = tile_base(tile, g);
+      const int m = p & (kTcM - 1);
+      const float2 *src = v + base + col_off[m];
       float2 x[S::UPT][4];
 #pragma unroll
       for (int i = 0; i < S::UPT; i++) {
-        int m, j;
-        unit_coords<KA, COL_FAST>(p + i * kTcProdThreads, m, j);
-        const float2 *src = v + base + col_off[m];
+        const int j = (p >> 7) + 2 * i;  // unit: block rows 4j .. 4j+3
+        if (PAIR) {
+          const float4 a = *reinterpret_cast<const float4 *>(src + blk_off[4 * j]);
+          const float4 b = *reinterpret_cast<const float4 *>(src + blk_off[4 * j + 2]);
+          x[i][0] = make_float2(a.x, a.y);
+          x[i][1] = make_float2(a.z, a.w);
+          x[i][2] = make_float2(b.x, b.y);
+          x[i][3] = make_float2(b.z, b.w);
+        } else {
 #pragma unroll
-        for (int e = 0; e < 4; e++) x[i][e] = src[blk_off[4 * j + e]];
+          for (int e = 0; e < 4; e++) x[i][e] = src[blk_off[4 * j + e]];
+        }
       }
       if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
       uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
@@ -307,10 +311,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       float part_all = 0.f;
 #pragma unroll
       for (int i = 0; i < S::UPT; i++) {
-        int m, j;
-        unit_coords<KA, COL_FAST>(p + i * kTcProdThreads, m, j);
+        const int j = (p >> 7) + 2 * i;
         uint32_t h[4], l[4];
-        float part = 0.f;
 #pragma unroll
         for (int e = 0; e < 4; e++) {
           __nv_bfloat162 hb = __floats2bfloat162_rn(x[i][e].x, x[i][e].y);
@@ -318,24 +320,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           __nv_bfloat162 lb = __floats2bfloat162_rn(x[i][e].x - hf.x, x[i][e].y - hf.y);
           h[e] = *reinterpret_cast<uint32_t *>(&hb);
           l[e] = *reinterpret_cast<uint32_t *>(&lb);
-          part += x[i][e].x * x[i][e].x + x[i][e].y * x[i][e].y;
+          part_all += x[i][e].x * x[i][e].x + x[i][e].y * x[i][e].y;
         }
         const int off = sw128_offset(m, 8 * j, kTcM);
         *reinterpret_cast<uint4 *>(ahi + off) = make_uint4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<uint4 *>(alo + off) = make_uint4(l[0], l[1], l[2], l[3]);
-        if (COL_FAST) {
-          part_all += part;  // every unit of this thread is in column p & 127
-        } else {
-          constexpr int G = KA / 4;  // consecutive lanes holding one column
-#pragma unroll
-          for (int o = G / 2; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-          if ((p & (G - 1)) == 0) {
-            sq[m] = part;
-            sq[kTcM + m] = 0.f;
-          }
-        }
       }
-      if (COL_FAST) sq[(p >> 7) * kTcM + (p & (kTcM - 1))] = part_all;
+      // threads p and p + 128 hold the two halves of column m's norm
+      sq[(p >> 7) * kTcM + m] = part_all;
       fence_async_shared();
       mbar_arrive(bar(stage));
       mbar_arrive(bar(7 + it % kSqSlots));
@@ -407,342 +399,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (int c = 0; c < S::N / 32; c++) {
         float acc[32];
         tmem_ld32(tb + 32 * c, acc);
+        if (PAIR) {
 #pragma unroll
-        for (int q = 0; q < 16; q++)
-          dst[blk_off[16 * c + q]] = make_float2(acc[2 * q] * scale, acc[2 * q + 1] * scale);
-      }
-      tc_fence_before();
-      mbar_arrive(bar(4 + stage));
-    }
-  }
-
-  tc_fence_before();
-  __syncthreads();
-  if (warp == kTcMmaWarp) {
-    tc_fence_after();
-    tmem_dealloc(tmem, S::TMEM_COLS);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// TMA-staged variant.
-//
-// The LSU-staged kernel above moves every amplitude through per-thread
-// 8-byte global loads and stores; ncu shows its L1/LSU path at 96 % while
-// HBM runs at a third of peak.  Here the tile's contiguous runs (>= 128
-// amplitudes, 1 KB) travel by cp.async.bulk between HBM and a stage buffer in
-// global order, so global traffic bypasses the LSU:
-//   loader (warp 13)     bulk-load tile t into stage buffer t % 2;
-//   converters (4-11)    read the fp32 tile from the buffer, split to bf16
-//                        hi/lo and write the swizzled A operand in place;
-//   MMA (warp 12)        as before;
-//   epilogue (0-3)       TMEM -> renormalised fp32 written into the same
-//                        buffer in global order, then one thread bulk-stores
-//                        the runs and releases the buffer to the loader.
-// Groups that meet at a named barrier take every wait decision through one
-// elected thread (bounded mbarrier wait, result broadcast through shared
-// memory), so an abort can never leave part of a group at the barrier.
-// ---------------------------------------------------------------------------
-
-constexpr int kTmaThreads = 448;  // 14 warps: + one loader warp
-constexpr int kTmaLoaderWarp = 13;
-
-struct TcGeomTma {
-  i64 n_tiles;
-  int nfree;
-  int nruns;       // contiguous runs per tile
-  int run_amps;    // amplitudes per run
-  signed char freeq[40];
-  i64 run_off[64];      // offset of run j from the tile base
-  int lpos_col[kTcM];   // position of column m in the tile's global order
-  int lpos_blk[64];     // position of block amplitude a
-};
-
-__device__ __forceinline__ void named_sync(int id, int nthreads) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes,
-                                          uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(dst),
-      "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void bulk_store(void *dst, uint32_t src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_commit() {
-  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void bulk_wait_read() {
-  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-}
-__device__ __forceinline__ void bulk_wait_all() {
-  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-}
-
-__device__ __forceinline__ i64 tile_base_tma(i64 tile, const TcGeomTma &g) {
-  i64 b = 0;
-  for (int j = 0; j < g.nfree; j++) b |= ((tile >> j) & 1LL) << g.freeq[j];
-  return b;
-}
-
-// Elected bounded wait for a group: thread `leader` waits, everyone learns
-// the outcome at the named barrier; on success every thread then observes
-// the completed phase itself (acquire), which returns at once.
-__device__ __forceinline__ bool group_wait(uint32_t bar, uint32_t parity, bool leader,
-                                           volatile int *flag, int bar_id, int nthreads,
-                                           volatile int *abort_flag, int *err, int where) {
-  if (leader) *flag = wait_bar(bar, parity, abort_flag, err, where) ? 1 : 0;
-  named_sync(bar_id, nthreads);
-  const bool ok = *flag != 0;
-  named_sync(bar_id, nthreads);  // the flag may be rewritten only after all read it
-  if (ok) mbar_try_wait(bar, parity);
-  return ok;
-}
-
-template <int KA, bool COL_FAST>
-__global__ void __launch_bounds__(kTmaThreads, 1)
-    k_block_tc_tma(float2 *v, const __grid_constant__ TcGeomTma g, const uint4 *bimg, int renorm,
-                   int *err) {
-  using S = TcShape<KA>;
-  constexpr int STAGE = 2 * S::A_BYTES;  // = 128 columns x KA amplitudes x 8 B
-  extern __shared__ uint8_t smem_dyn[];
-  const uint32_t raw = smem_u32(smem_dyn);
-  uint8_t *smem = smem_dyn + ((1024u - (raw & 1023u)) & 1023u);
-  uint8_t *sA = smem + S::OFF_A;  // two stage buffers
-  uint8_t *sB = smem + S::OFF_B;
-  int *lpos_col = reinterpret_cast<int *>(smem + S::OFF_COL);        // 128 ints
-  int *lpos_blk = reinterpret_cast<int *>(smem + S::OFF_COL + 512);  // 64 ints
-  float *colsq = reinterpret_cast<float *>(smem + S::OFF_SQ);
-  const uint32_t bar0 = smem_u32(smem + S::OFF_BAR);
-  // 0,1 a_full  2,3 mma_done  4,5 acc_empty  6 drain  7..10 sq_full
-  // 11,12 load_full  13,14 store_done
-  auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::OFF_MISC);
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::OFF_MISC + 4);
-  volatile int *conv_flag = reinterpret_cast<volatile int *>(smem + S::OFF_MISC + 8);
-  volatile int *epi_flag = reinterpret_cast<volatile int *>(smem + S::OFF_MISC + 12);
-
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (tid == 0) {
-    mbar_init(bar(0), kTcProdThreads);
-    mbar_init(bar(1), kTcProdThreads);
-    mbar_init(bar(2), 1);
-    mbar_init(bar(3), 1);
-    mbar_init(bar(4), kTcEpiThreads);
-    mbar_init(bar(5), kTcEpiThreads);
-    mbar_init(bar(6), 1);
-    for (int k = 0; k < kSqSlots; k++) mbar_init(bar(7 + k), kTcProdThreads);
-    mbar_init(bar(11), 1);
-    mbar_init(bar(12), 1);
-    mbar_init(bar(13), 1);
-    mbar_init(bar(14), 1);
-    *abort_flag = 0;
-    fence_barrier_init();
-  }
-  for (int i = tid; i < kTcM; i += kTmaThreads) lpos_col[i] = g.lpos_col[i];
-  for (int i = tid; i < KA; i += kTmaThreads) lpos_blk[i] = g.lpos_blk[i];
-  {
-    uint4 *dst = reinterpret_cast<uint4 *>(sB);
-    for (int i = tid; i < S::IMG_BYTES / 16; i += kTmaThreads) dst[i] = bimg[i];
-  }
-  fence_async_shared();
-  if (warp == kTcMmaWarp) {
-    tmem_alloc(smem_u32(tmem_slot), S::TMEM_COLS);
-    tmem_relinquish();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-  const uint32_t run_bytes = (uint32_t)g.run_amps * 8u;
-
-  if (warp == kTmaLoaderWarp) {
-    // ---------------- TMA loader ----------------
-    if (lane == 0) {
-      int it = 0;
-      for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
-        const int stage = it & 1;
-        if (it >= 2 && !wait_bar(bar(13 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 7)) break;
-        const i64 base = tile_base_tma(tile, g);
-        const uint32_t dst = smem_u32(sA + stage * STAGE);
-        mbar_expect_tx(bar(11 + stage), (uint32_t)STAGE);
-        for (int j = 0; j < g.nruns; j++)
-          bulk_load(dst + (uint32_t)j * run_bytes, v + base + g.run_off[j], run_bytes, bar(11 + stage));
-      }
-      // On an abort the converters may not consume the last loads: wait
-      // (bounded, whatever the abort flag says) until they have landed
-      // before the CTA can exit.
-      for (int back = 1; back <= 2 && it - back >= 0; back++) {
-        const int lt = it - back;
-        long long t0 = clock64();
-        while (!mbar_try_wait(bar(11 + (lt & 1)), (lt >> 1) & 1)) {
-          if (clock64() - t0 > kWaitCycles) {
-            atomicExch(err, 9);
-            break;
-          }
-        }
-      }
-    }
-    __syncwarp();
-  } else if (warp >= kTcEpiWarps && warp < kTcMmaWarp) {
-    // ---------------- converters ----------------
-    const int p = tid - kTcEpiThreads;
-    const bool leader = p == 0;
-    int it = 0;
-    for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
-      const int stage = it & 1;
-      if (!group_wait(bar(11 + stage), (it >> 1) & 1, leader, conv_flag, 1, kTcProdThreads,
-                      abort_flag, err, 8))
-        break;
-      const float2 *stg = reinterpret_cast<const float2 *>(sA + stage * STAGE);
-      float2 x[S::UPT][4];
-#pragma unroll
-      for (int i = 0; i < S::UPT; i++) {
-        int m, j;
-        unit_coords<KA, COL_FAST>(p + i * kTcProdThreads, m, j);
-        const int cm = lpos_col[m];
-#pragma unroll
-        for (int e = 0; e < 4; e++) x[i][e] = stg[cm + lpos_blk[4 * j + e]];
-      }
-      named_sync(1, kTcProdThreads);  // all reads done: the buffer becomes the A operand
-      uint8_t *ahi = sA + stage * STAGE;
-      uint8_t *alo = ahi + S::A_BYTES;
-      float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
-      float part_all = 0.f;
-#pragma unroll
-      for (int i = 0; i < S::UPT; i++) {
-        int m, j;
-        unit_coords<KA, COL_FAST>(p + i * kTcProdThreads, m, j);
-        uint32_t h[4], l[4];
-        float part = 0.f;
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-          __nv_bfloat162 hb = __floats2bfloat162_rn(x[i][e].x, x[i][e].y);
-          float2 hf = __bfloat1622float2(hb);
-          __nv_bfloat162 lb = __floats2bfloat162_rn(x[i][e].x - hf.x, x[i][e].y - hf.y);
-          h[e] = *reinterpret_cast<uint32_t *>(&hb);
-          l[e] = *reinterpret_cast<uint32_t *>(&lb);
-          part += x[i][e].x * x[i][e].x + x[i][e].y * x[i][e].y;
-        }
-        const int off = sw128_offset(m, 8 * j, kTcM);
-        *reinterpret_cast<uint4 *>(ahi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4 *>(alo + off) = make_uint4(l[0], l[1], l[2], l[3]);
-        if (COL_FAST) {
-          part_all += part;
+          for (int q = 0; q < 8; q++)
+            *reinterpret_cast<float4 *>(dst + blk_off[16 * c + 2 * q]) =
+                make_float4(acc[4 * q] * scale, acc[4 * q + 1] * scale, acc[4 * q + 2] * scale,
+                            acc[4 * q + 3] * scale);
         } else {
-          constexpr int G = KA / 4;
 #pragma unroll
-          for (int o = G / 2; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-          if ((p & (G - 1)) == 0) {
-            sq[m] = part;
-            sq[kTcM + m] = 0.f;
-          }
+          for (int q = 0; q < 16; q++)
+            dst[blk_off[16 * c + q]] = make_float2(acc[2 * q] * scale, acc[2 * q + 1] * scale);
         }
-      }
-      if (COL_FAST) sq[(p >> 7) * kTcM + (p & (kTcM - 1))] = part_all;
-      fence_async_shared();
-      mbar_arrive(bar(stage));
-      mbar_arrive(bar(7 + it % kSqSlots));
-    }
-  } else if (warp == kTcMmaWarp) {
-    // ---------------- MMA issue ----------------
-    if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16(kTcM, S::N);
-      const uint32_t a0 = smem_u32(sA), b_hi = smem_u32(sB), b_lo = b_hi + S::B_BYTES;
-      int it = 0;
-      for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
-        const int stage = it & 1;
-        if (!wait_bar(bar(stage), (it >> 1) & 1, abort_flag, err, 2)) break;
-        if (it >= 2 && !wait_bar(bar(4 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 3)) break;
-        tc_fence_after();
-        const uint32_t d = tmem + (uint32_t)(stage * S::N);
-        const uint32_t a_hi = a0 + (uint32_t)(stage * STAGE);
-        const uint32_t a_lo = a_hi + S::A_BYTES;
-#pragma unroll
-        for (int s = 0; s < S::KSTEPS; s++) {
-          const uint32_t ka = (uint32_t)((s >> 2) * (kTcM * 128) + (s & 3) * 32);
-          const uint32_t kb = (uint32_t)((s >> 2) * (S::N * 128) + (s & 3) * 32);
-          umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_hi + kb), idesc, s > 0 ? 1u : 0u);
-          umma_bf16(d, sw128_desc(a_hi + ka), sw128_desc(b_lo + kb), idesc, 1u);
-          umma_bf16(d, sw128_desc(a_lo + ka), sw128_desc(b_hi + kb), idesc, 1u);
-        }
-        umma_commit(bar(2 + stage));
-      }
-      umma_commit(bar(6));
-      long long t0 = clock64();
-      while (!mbar_try_wait(bar(6), 0)) {
-        if (clock64() - t0 > kWaitCycles) {
-          atomicExch(err, 4);
-          break;
-        }
-      }
-    }
-    __syncwarp();
-  } else {
-    // ---------------- epilogue ----------------
-    const int m = tid;
-    const bool leader = tid == 0;
-    const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
-    int it = 0;
-    for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
-      const int stage = it & 1;
-      if (!group_wait(bar(2 + stage), (it >> 1) & 1, leader, epi_flag, 2, kTcEpiThreads,
-                      abort_flag, err, 5))
-        break;
-      if (!group_wait(bar(7 + it % kSqSlots), (it / kSqSlots) & 1, leader, epi_flag, 2,
-                      kTcEpiThreads, abort_flag, err, 6))
-        break;
-      tc_fence_after();
-      const uint32_t tb = tmem + lane_addr + (uint32_t)(stage * S::N);
-      float scale = 1.f;
-      if (renorm) {
-        float out = 0.f;
-#pragma unroll 1
-        for (int c = 0; c < S::N / 32; c++) {
-          float acc[32];
-          tmem_ld32(tb + 32 * c, acc);
-#pragma unroll
-          for (int q = 0; q < 32; q++) out += acc[q] * acc[q];
-        }
-        const float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
-        const float in = sq[m] + sq[kTcM + m];
-        if (out > 0.f) scale = sqrtf(in / out);
-      }
-      // the stage buffer is dead as an operand once the MMAs completed
-      float2 *stg = reinterpret_cast<float2 *>(sA + stage * STAGE);
-      const int cm = lpos_col[m];
-#pragma unroll 1
-      for (int c = 0; c < S::N / 32; c++) {
-        float acc[32];
-        tmem_ld32(tb + 32 * c, acc);
-#pragma unroll
-        for (int q = 0; q < 16; q++)
-          stg[cm + lpos_blk[16 * c + q]] = make_float2(acc[2 * q] * scale, acc[2 * q + 1] * scale);
       }
       tc_fence_before();
       mbar_arrive(bar(4 + stage));
-      fence_async_shared();             // the buffer is read by the bulk store
-      named_sync(2, kTcEpiThreads);
-      if (leader) {
-        const i64 base = tile_base_tma(tile, g);
-        const uint32_t src = smem_u32(sA + stage * STAGE);
-        for (int j = 0; j < g.nruns; j++)
-          bulk_store(v + base + g.run_off[j], src + (uint32_t)j * run_bytes, run_bytes);
-        bulk_commit();
-        bulk_wait_read();               // the buffer may be refilled once read
-        mbar_arrive(bar(13 + stage));
-      }
     }
-    if (leader) bulk_wait_all();
   }
 
   tc_fence_before();
@@ -833,41 +504,12 @@ bool tc_supported(const qcs_cuda_state *s, int k) {
          s->n >= k + 7 && s->n - k - 7 <= 40 && s->dev.cc_major == 10 && s->dev.cc_minor == 3;
 }
 
-template <int KA, bool COL_FAST>
-static int launch_tc_tma(qcs_cuda_state *s, const TcGeomTma &g, const uint4 *img, int renorm) {
-  using S = TcShape<KA>;
-  static bool configured = false;
-  if (!configured) {
-    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc_tma<KA, COL_FAST>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM),
-                        "cudaFuncSetAttribute(tcgen05 block, TMA)");
-    if (rc) return rc;
-    configured = true;
-  }
-  const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
-  prof_begin(s);
-  k_block_tc_tma<KA, COL_FAST><<<grid, kTmaThreads, S::SMEM, s->stream>>>(
-      (float2 *)s->vec, g, img, renorm, s->d_err);
-  return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05, TMA)");
-}
-
-// QCS_TC_STAGING=lsu selects the per-thread-load variant (kept for
-// comparison); the TMA-staged variant is the default.
-static bool use_tma_staging() {
-  static int v = -1;
-  if (v < 0) {
-    const char *e = getenv("QCS_TC_STAGING");
-    v = (e && strcmp(e, "lsu") == 0) ? 0 : 1;
-  }
-  return v == 1;
-}
-
-template <int KA, bool COL_FAST>
+template <int KA, bool PAIR>
 static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int renorm) {
   using S = TcShape<KA>;
   static bool configured = false;
   if (!configured) {
-    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc<KA, COL_FAST>,
+    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc<KA, PAIR>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM),
                         "cudaFuncSetAttribute(tcgen05 block)");
     if (rc) return rc;
@@ -875,7 +517,7 @@ static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int r
   }
   const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
   prof_begin(s);
-  k_block_tc<KA, COL_FAST><<<grid, kTcThreads, S::SMEM, s->stream>>>(
+  k_block_tc<KA, PAIR><<<grid, kTcThreads, S::SMEM, s->stream>>>(
       (float2 *)s->vec, g, img, renorm, s->d_err);
   return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
 }
@@ -899,11 +541,41 @@ static double unitarity_defect(const double *u, int K) {
   return worst;
 }
 
-int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u,
+int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double *u_in,
                    bool known_unitary) {
   int rc = ring_init(s);
   if (rc) return rc;
   TcRing *r = s->tc;
+  const int KA = 1 << k;
+  // Ascending qubits (block bit j = j-th smallest qubit), the matrix relabelled
+  // to match: new index a' has bit j where the old index has bit order[j].
+  int order[8], qubits[8];
+  for (int j = 0; j < k; j++) order[j] = j;
+  std::sort(order, order + k, [&](int x, int y) { return qubits_in[x] < qubits_in[y]; });
+  bool sorted = true;
+  for (int j = 0; j < k; j++) {
+    qubits[j] = qubits_in[order[j]];
+    sorted = sorted && order[j] == j;
+  }
+  std::vector<double> u_perm;
+  const double *u = u_in;
+  if (!sorted) {
+    std::vector<int> old_of(KA);
+    for (int a = 0; a < KA; a++) {
+      int o = 0;
+      for (int j = 0; j < k; j++)
+        if ((a >> j) & 1) o |= 1 << order[j];
+      old_of[a] = o;
+    }
+    u_perm.resize((size_t)2 * KA * KA);
+    for (int a = 0; a < KA; a++)
+      for (int b = 0; b < KA; b++) {
+        const size_t src = 2 * ((size_t)old_of[a] * KA + old_of[b]);
+        u_perm[2 * ((size_t)a * KA + b)] = u_in[src];
+        u_perm[2 * ((size_t)a * KA + b) + 1] = u_in[src + 1];
+      }
+    u = u_perm.data();
+  }
   // geometry
   TcGeom g;
   memset(&g, 0, sizeof(g));
@@ -924,14 +596,13 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u,
       if ((m >> b) & 1) o |= 1LL << colq[b];
     g.col_off[m] = o;
   }
-  const int KA = 1 << k;
   for (int a = 0; a < KA; a++) {
     i64 o = 0;
     for (int j = 0; j < k; j++)
       if ((a >> j) & 1) o |= 1LL << qubits[j];
     g.blk_off[a] = o;
   }
-  const bool col_fast = role[0] == -2;
+  const bool pair = qubits[0] == 0;  // qubit 0 is block bit 0
   // block-matrix image through the pinned ring
   const int slot = r->next;
   r->next = (r->next + 1) % kImgSlots;
@@ -948,55 +619,10 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u,
   if (rc) return rc;
   const uint4 *img = reinterpret_cast<const uint4 *>(d);
   const int renorm = (known_unitary || unitarity_defect(u, KA) < 1e-9) ? 1 : 0;
-  if (use_tma_staging()) {
-    // tile positions in global order: bit m of the local index is qubit tq[m]
-    TcGeomTma t;
-    memset(&t, 0, sizeof(t));
-    std::vector<int> tq;
-    for (int q = 0; q < s->n; q++)
-      if (role[q] != -1) tq.push_back(q);
-    const int nT = (int)tq.size();  // k + 7
-    int rl = 0;
-    while (rl < nT && tq[rl] == rl) rl++;  // tile bits 0..rl-1 are qubits 0..rl-1
-    t.n_tiles = g.n_tiles;
-    t.nfree = g.nfree;
-    memcpy(t.freeq, g.freeq, sizeof(t.freeq));
-    t.run_amps = 1 << rl;
-    t.nruns = 1 << (nT - rl);
-    for (int j = 0; j < t.nruns; j++) {
-      i64 o = 0;
-      for (int b = rl; b < nT; b++)
-        if ((j >> (b - rl)) & 1) o |= 1LL << tq[b];
-      t.run_off[j] = o;
-    }
-    auto local_pos = [&](int q) {
-      for (int b = 0; b < nT; b++)
-        if (tq[b] == q) return 1 << b;
-      return 0;
-    };
-    for (int m = 0; m < kTcM; m++) {
-      int pos = 0;
-      for (int b = 0; b < 7; b++)
-        if ((m >> b) & 1) pos += local_pos(colq[b]);
-      t.lpos_col[m] = pos;
-    }
-    for (int a = 0; a < KA; a++) {
-      int pos = 0;
-      for (int j = 0; j < k; j++)
-        if ((a >> j) & 1) pos += local_pos(qubits[j]);
-      t.lpos_blk[a] = pos;
-    }
-    if (k == 6)
-      rc = col_fast ? launch_tc_tma<64, true>(s, t, img, renorm) : launch_tc_tma<64, false>(s, t, img, renorm);
-    else
-      rc = col_fast ? launch_tc_tma<32, true>(s, t, img, renorm) : launch_tc_tma<32, false>(s, t, img, renorm);
-    if (rc) return rc;
-    return check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
-  }
   if (k == 6)
-    rc = col_fast ? launch_tc<64, true>(s, g, img, renorm) : launch_tc<64, false>(s, g, img, renorm);
+    rc = pair ? launch_tc<64, true>(s, g, img, renorm) : launch_tc<64, false>(s, g, img, renorm);
   else
-    rc = col_fast ? launch_tc<32, true>(s, g, img, renorm) : launch_tc<32, false>(s, g, img, renorm);
+    rc = pair ? launch_tc<32, true>(s, g, img, renorm) : launch_tc<32, false>(s, g, img, renorm);
   if (rc) return rc;
   return check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
 }
