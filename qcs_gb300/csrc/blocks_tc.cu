@@ -61,6 +61,19 @@ constexpr int kTcEpiThreads = kTcEpiWarps * 32;          // 128
 constexpr long long kWaitCycles = 4000000000LL;          // ~2 s at 2 GHz
 constexpr int kImgSlots = 8;                             // block-matrix upload ring
 constexpr int kSqSlots = 4;                              // column-norm ring
+constexpr int kEpiPitch = 33;  // floats per staged column (conflict-free transpose)
+
+// Memory access modes of the kernel (chosen per block on the host):
+//   kColMode   qubit 0 is a column qubit: a warp's 32 columns are adjacent
+//              amplitudes, one 8-byte access per amplitude;
+//   kPairMode  qubit 0 is block qubit 0: block rows 2b, 2b+1 of a column are
+//              adjacent and move as one 16-byte access;
+//   kLowMode   the block is exactly qubits 0..k-1: a column is 2^k adjacent
+//              amplitudes and the tile one contiguous 128 * 2^k run; a warp
+//              loads 512 contiguous bytes per instruction and the epilogue
+//              transposes each 32 x 32 result block through shared memory,
+//              so that its stores are contiguous too.
+constexpr int kColMode = 0, kPairMode = 1, kLowMode = 2;
 
 template <int KA>  // amplitudes per column (2^k)
 struct TcShape {
@@ -77,7 +90,8 @@ struct TcShape {
   static constexpr int OFF_COL = OFF_B + 2 * B_BYTES;
   static constexpr int OFF_BLK = OFF_COL + kTcM * 8;
   static constexpr int OFF_SQ = OFF_BLK + KA * 8;  // float [slot 4][half][column]
-  static constexpr int OFF_BAR = OFF_SQ + kSqSlots * 2 * kTcM * 4;
+  static constexpr int OFF_EPI = OFF_SQ + kSqSlots * 2 * kTcM * 4;  // LOW mode staging
+  static constexpr int OFF_BAR = OFF_EPI + kTcEpiWarps * 32 * kEpiPitch * 4;
   static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
   static constexpr int SMEM = OFF_MISC + 16 + 1024;  // + slack to align the base to 1 KB
   static constexpr int IMG_BYTES = 2 * B_BYTES;
@@ -220,12 +234,9 @@ __device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
   return b;
 }
 
-// PAIR: qubit 0 is block bit 0, so block rows 2b and 2b+1 of a column are
-// adjacent amplitudes and move as one 16-byte access.  Otherwise qubit 0 is
-// column bit 0 and a warp's 32 columns are (mostly) adjacent amplitudes.
-// Either way a producer thread keeps one column (tile row m = p % 128) and
-// consecutive threads take consecutive columns.
-template <int KA, bool PAIR>
+// In kColMode and kPairMode a producer thread keeps one column (tile row
+// m = p % 128) and consecutive threads take consecutive columns.
+template <int KA, int MODE>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_block_tc(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
                int *err) {
@@ -238,6 +249,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   i64 *col_off = reinterpret_cast<i64 *>(smem + S::OFF_COL);
   i64 *blk_off = reinterpret_cast<i64 *>(smem + S::OFF_BLK);
   float *colsq = reinterpret_cast<float *>(smem + S::OFF_SQ);
+  float *epi = reinterpret_cast<float *>(smem + S::OFF_EPI);
   const uint32_t bar0 = smem_u32(smem + S::OFF_BAR);  // 8-byte barriers:
   // 0,1 a_full[stage]  2,3 mma_done[stage]  4,5 acc_empty[stage]  6 drain
   // 7..10 sq_full[slot]: a tile's column norms are in colsq[slot]
@@ -286,13 +298,75 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
       const int stage = it & 1;
       const i64 base = tile_base(tile, g);
+      if constexpr (MODE == kLowMode) {
+        // warp pw loads 512 contiguous bytes per step: CPS columns of KA
+        // amplitudes; lane l holds rows 2r, 2r+1 of column cb + l / LPC
+        constexpr int CPS = 64 / KA;           // columns per step (1 or 2)
+        constexpr int LPC = 32 / CPS;          // lanes per column
+        constexpr int STEPS = kTcM / (kTcProdWarps * CPS);
+        const int pw = p >> 5;
+        const int r2 = 2 * (lane % LPC);       // first of the lane's two rows
+        float4 x[STEPS];
+#pragma unroll
+        for (int i = 0; i < STEPS; i++) {
+          const int m = (pw * STEPS + i) * CPS + lane / LPC;
+          x[i] = *reinterpret_cast<const float4 *>(v + base + col_off[m] + r2);
+        }
+        if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
+        uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
+        uint8_t *alo = ahi + S::A_BYTES;
+        float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
+        float part[STEPS];
+#pragma unroll
+        for (int i = 0; i < STEPS; i++) {
+          const int m = (pw * STEPS + i) * CPS + lane / LPC;
+          __nv_bfloat162 h0 = __floats2bfloat162_rn(x[i].x, x[i].y);
+          __nv_bfloat162 h1 = __floats2bfloat162_rn(x[i].z, x[i].w);
+          const float2 f0 = __bfloat1622float2(h0), f1 = __bfloat1622float2(h1);
+          __nv_bfloat162 l0 = __floats2bfloat162_rn(x[i].x - f0.x, x[i].y - f0.y);
+          __nv_bfloat162 l1 = __floats2bfloat162_rn(x[i].z - f1.x, x[i].w - f1.y);
+          const int off = sw128_offset(m, 2 * r2, kTcM);
+          *reinterpret_cast<uint2 *>(ahi + off) =
+              make_uint2(*reinterpret_cast<uint32_t *>(&h0), *reinterpret_cast<uint32_t *>(&h1));
+          *reinterpret_cast<uint2 *>(alo + off) =
+              make_uint2(*reinterpret_cast<uint32_t *>(&l0), *reinterpret_cast<uint32_t *>(&l1));
+          part[i] = x[i].x * x[i].x + x[i].y * x[i].y + x[i].z * x[i].z + x[i].w * x[i].w;
+        }
+        // Column norms: part[i] of lane l belongs to the warp's column
+        // i * CPS + l / LPC.  A reduce-scatter over the LPC lanes of each
+        // column (fixed order, deterministic): after the step with offset o
+        // a lane keeps the half of its values selected by (l & o), so lane
+        // bits 1.. select the surviving column; a last exchange with the
+        // neighbour lane completes the sum.
+        constexpr int LOG_STEPS = STEPS == 16 ? 4 : 3;
+        static_assert(STEPS == (1 << LOG_STEPS) && STEPS * 2 == LPC, "reduce-scatter shape");
+#pragma unroll
+        for (int st = 0; st < LOG_STEPS; st++) {
+          const int o = LPC >> (st + 1);
+          const int half = STEPS >> (st + 1);
+          const bool up = (lane & o) != 0;
+#pragma unroll
+          for (int j = 0; j < half; j++) {
+            const float send = up ? part[j] : part[half + j];
+            const float keep = up ? part[half + j] : part[j];
+            part[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+          }
+        }
+        part[0] += __shfl_xor_sync(0xffffffffu, part[0], 1);
+        if ((lane & 1) == 0) {
+          const int i_sel = (lane % LPC) >> 1;
+          const int m = (pw * STEPS + i_sel) * CPS + lane / LPC;
+          sq[m] = part[0];
+          sq[kTcM + m] = 0.f;
+        }
+      } else {
       const int m = p & (kTcM - 1);
       const float2 *src = v + base + col_off[m];
       float2 x[S::UPT][4];
 #pragma unroll
       for (int i = 0; i < S::UPT; i++) {
         const int j = (p >> 7) + 2 * i;  // unit: block rows 4j .. 4j+3
-        if (PAIR) {
+        if constexpr (MODE == kPairMode) {
           const float4 a = *reinterpret_cast<const float4 *>(src + blk_off[4 * j]);
           const float4 b = *reinterpret_cast<const float4 *>(src + blk_off[4 * j + 2]);
           x[i][0] = make_float2(a.x, a.y);
@@ -328,6 +402,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       // threads p and p + 128 hold the two halves of column m's norm
       sq[(p >> 7) * kTcM + m] = part_all;
+      }
       fence_async_shared();
       mbar_arrive(bar(stage));
       mbar_arrive(bar(7 + it % kSqSlots));
@@ -394,12 +469,33 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const float in = sq[m] + sq[kTcM + m];
         if (out > 0.f) scale = sqrtf(in / out);
       }
-      float2 *dst = v + tile_base(tile, g) + col_off[m];
+      const i64 base = tile_base(tile, g);
+      if constexpr (MODE == kLowMode) {
+        // Result block c of this warp: 32 columns x 32 reals (rows 16c ..
+        // 16c+15), transposed through shared memory so that each store
+        // instruction writes one column's 16 adjacent amplitudes (128 B).
+        float *buf = epi + warp * 32 * kEpiPitch;
+#pragma unroll 1
+        for (int c = 0; c < S::N / 32; c++) {
+          float acc[32];
+          tmem_ld32(tb + 32 * c, acc);
+#pragma unroll
+          for (int q = 0; q < 32; q++) buf[lane * kEpiPitch + q] = acc[q] * scale;
+          __syncwarp();
+#pragma unroll 4
+          for (int j = 0; j < 32; j++) {
+            float *col = reinterpret_cast<float *>(v + base + col_off[warp * 32 + j] + 16 * c);
+            col[lane] = buf[j * kEpiPitch + lane];
+          }
+          __syncwarp();
+        }
+      } else {
+      float2 *dst = v + base + col_off[m];
 #pragma unroll 1
       for (int c = 0; c < S::N / 32; c++) {
         float acc[32];
         tmem_ld32(tb + 32 * c, acc);
-        if (PAIR) {
+        if constexpr (MODE == kPairMode) {
 #pragma unroll
           for (int q = 0; q < 8; q++)
             *reinterpret_cast<float4 *>(dst + blk_off[16 * c + 2 * q]) =
@@ -410,6 +506,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           for (int q = 0; q < 16; q++)
             dst[blk_off[16 * c + q]] = make_float2(acc[2 * q] * scale, acc[2 * q + 1] * scale);
         }
+      }
       }
       tc_fence_before();
       mbar_arrive(bar(4 + stage));
@@ -504,12 +601,12 @@ bool tc_supported(const qcs_cuda_state *s, int k) {
          s->n >= k + 7 && s->n - k - 7 <= 40 && s->dev.cc_major == 10 && s->dev.cc_minor == 3;
 }
 
-template <int KA, bool PAIR>
+template <int KA, int MODE>
 static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int renorm) {
   using S = TcShape<KA>;
   static bool configured = false;
   if (!configured) {
-    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc<KA, PAIR>,
+    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc<KA, MODE>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM),
                         "cudaFuncSetAttribute(tcgen05 block)");
     if (rc) return rc;
@@ -517,7 +614,7 @@ static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int r
   }
   const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
   prof_begin(s);
-  k_block_tc<KA, PAIR><<<grid, kTcThreads, S::SMEM, s->stream>>>(
+  k_block_tc<KA, MODE><<<grid, kTcThreads, S::SMEM, s->stream>>>(
       (float2 *)s->vec, g, img, renorm, s->d_err);
   return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
 }
@@ -602,7 +699,9 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
       if ((a >> j) & 1) o |= 1LL << qubits[j];
     g.blk_off[a] = o;
   }
-  const bool pair = qubits[0] == 0;  // qubit 0 is block bit 0
+  bool low = true;  // the block is exactly qubits 0..k-1
+  for (int j = 0; j < k; j++) low = low && qubits[j] == j;
+  const int mode = low ? kLowMode : (qubits[0] == 0 ? kPairMode : kColMode);
   // block-matrix image through the pinned ring
   const int slot = r->next;
   r->next = (r->next + 1) % kImgSlots;
@@ -620,9 +719,13 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
   const uint4 *img = reinterpret_cast<const uint4 *>(d);
   const int renorm = (known_unitary || unitarity_defect(u, KA) < 1e-9) ? 1 : 0;
   if (k == 6)
-    rc = pair ? launch_tc<64, true>(s, g, img, renorm) : launch_tc<64, false>(s, g, img, renorm);
+    rc = mode == kLowMode    ? launch_tc<64, kLowMode>(s, g, img, renorm)
+         : mode == kPairMode ? launch_tc<64, kPairMode>(s, g, img, renorm)
+                             : launch_tc<64, kColMode>(s, g, img, renorm);
   else
-    rc = pair ? launch_tc<32, true>(s, g, img, renorm) : launch_tc<32, false>(s, g, img, renorm);
+    rc = mode == kLowMode    ? launch_tc<32, kLowMode>(s, g, img, renorm)
+         : mode == kPairMode ? launch_tc<32, kPairMode>(s, g, img, renorm)
+                             : launch_tc<32, kColMode>(s, g, img, renorm);
   if (rc) return rc;
   return check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
 }

@@ -302,14 +302,20 @@ TC_ATOL = 5e-5
 
 
 @pytest.mark.parametrize("k", [5, 6])
-@pytest.mark.parametrize("with_q0", [False, True])
-def test_apply_block_tensor_cores(k, with_q0):
+@pytest.mark.parametrize("placement", ["col", "pair", "low"])
+def test_apply_block_tensor_cores(k, placement):
+    """The kernel's three access modes: qubit 0 a column qubit, qubit 0 in the
+    block, the block exactly qubits 0..k-1; qubits in random order."""
     n = 15
-    rng = np.random.default_rng(10 * k + with_q0)
+    rng = np.random.default_rng(10 * k + len(placement))
     for trial in range(3):
         rest = [q for q in range(1, n)]
-        qubits = list(rng.choice(rest, size=k - 1 if with_q0 else k, replace=False))
-        if with_q0:
+        if placement == "low":
+            qubits = [int(q) for q in rng.permutation(k)]
+        else:
+            qubits = list(rng.choice(rest, size=k - 1 if placement == "pair" else k,
+                                     replace=False))
+        if placement == "pair":
             qubits.insert(int(rng.integers(0, k)), 0)
         m = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
         u, _ = np.linalg.qr(m)
@@ -339,7 +345,8 @@ def test_tensor_cores_preserve_the_norm_over_many_blocks():
         for i in range(100):
             m = rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64))
             u, _ = np.linalg.qr(m)
-            qubits = list(rng.choice(n, size=6, replace=False))
+            qubits = (list(range(6)) if i % 5 == 0 else
+                      list(rng.choice(n, size=6, replace=False)))
             s.apply_block(qubits, u, capi.FUSE_TENSOR)
         s.synchronize()
         assert abs(s.norm_sq() - 1.0) < 1e-5
