@@ -293,45 +293,109 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // Column-norm slot it % 4 was last read by the epilogue of tile it-4,
     // which finished before the MMAs of tile it-2 could start (they wait for
     // its acc_empty), so the slot is free too.
+    // Loads run one tile ahead: a thread holds its share of a tile in two
+    // register halves; as soon as a half is converted into the operand, the
+    // same registers take the next tile's half, so the next tile's loads are
+    // in flight while this tile is converted and while the stage is awaited.
     const int p = tid - kTcEpiThreads;
-    int it = 0;
-    for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
-      const int stage = it & 1;
-      const i64 base = tile_base(tile, g);
+    constexpr int CPS = 64 / KA;           // kLowMode: columns per 512-byte step
+    constexpr int LPC = 32 / CPS;          // kLowMode: lanes per column
+    constexpr int STEPS = kTcM / (kTcProdWarps * CPS);
+    constexpr int HS = STEPS / 2;          // kLowMode: steps per half
+    constexpr int HU = S::UPT / 2;         // other modes: units per half
+    const int pw = p >> 5;
+    const int r2 = 2 * (lane % LPC);       // kLowMode: first of the lane's two rows
+    const int mc = p & (kTcM - 1);         // other modes: the thread's column
+    float4 xl[2][HS];                      // kLowMode data, by half
+    float2 xc[2][HU][4];                   // other modes' data, by half
+    auto load_half = [&](i64 base, int h) {
       if constexpr (MODE == kLowMode) {
-        // warp pw loads 512 contiguous bytes per step: CPS columns of KA
-        // amplitudes; lane l holds rows 2r, 2r+1 of column cb + l / LPC
-        constexpr int CPS = 64 / KA;           // columns per step (1 or 2)
-        constexpr int LPC = 32 / CPS;          // lanes per column
-        constexpr int STEPS = kTcM / (kTcProdWarps * CPS);
-        const int pw = p >> 5;
-        const int r2 = 2 * (lane % LPC);       // first of the lane's two rows
-        float4 x[STEPS];
 #pragma unroll
-        for (int i = 0; i < STEPS; i++) {
-          const int m = (pw * STEPS + i) * CPS + lane / LPC;
-          x[i] = *reinterpret_cast<const float4 *>(v + base + col_off[m] + r2);
+        for (int i = 0; i < HS; i++) {
+          const int m = (pw * STEPS + h * HS + i) * CPS + lane / LPC;
+          xl[h][i] = *reinterpret_cast<const float4 *>(v + base + col_off[m] + r2);
         }
-        if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
-        uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
-        uint8_t *alo = ahi + S::A_BYTES;
-        float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
-        float part[STEPS];
+      } else {
+        const float2 *src = v + base + col_off[mc];
 #pragma unroll
-        for (int i = 0; i < STEPS; i++) {
-          const int m = (pw * STEPS + i) * CPS + lane / LPC;
-          __nv_bfloat162 h0 = __floats2bfloat162_rn(x[i].x, x[i].y);
-          __nv_bfloat162 h1 = __floats2bfloat162_rn(x[i].z, x[i].w);
+        for (int i = 0; i < HU; i++) {
+          const int j = (p >> 7) + 2 * (h * HU + i);  // unit: block rows 4j .. 4j+3
+          if constexpr (MODE == kPairMode) {
+            const float4 a = *reinterpret_cast<const float4 *>(src + blk_off[4 * j]);
+            const float4 b = *reinterpret_cast<const float4 *>(src + blk_off[4 * j + 2]);
+            xc[h][i][0] = make_float2(a.x, a.y);
+            xc[h][i][1] = make_float2(a.z, a.w);
+            xc[h][i][2] = make_float2(b.x, b.y);
+            xc[h][i][3] = make_float2(b.z, b.w);
+          } else {
+#pragma unroll
+            for (int e = 0; e < 4; e++) xc[h][i][e] = src[blk_off[4 * j + e]];
+          }
+        }
+      }
+    };
+    float part[STEPS];  // kLowMode: per-step partial norms; [0]: other modes
+    auto convert_half = [&](int h, uint8_t *ahi, uint8_t *alo) {
+      if constexpr (MODE == kLowMode) {
+#pragma unroll
+        for (int i = 0; i < HS; i++) {
+          const float4 x = xl[h][i];
+          const int m = (pw * STEPS + h * HS + i) * CPS + lane / LPC;
+          __nv_bfloat162 h0 = __floats2bfloat162_rn(x.x, x.y);
+          __nv_bfloat162 h1 = __floats2bfloat162_rn(x.z, x.w);
           const float2 f0 = __bfloat1622float2(h0), f1 = __bfloat1622float2(h1);
-          __nv_bfloat162 l0 = __floats2bfloat162_rn(x[i].x - f0.x, x[i].y - f0.y);
-          __nv_bfloat162 l1 = __floats2bfloat162_rn(x[i].z - f1.x, x[i].w - f1.y);
+          __nv_bfloat162 l0 = __floats2bfloat162_rn(x.x - f0.x, x.y - f0.y);
+          __nv_bfloat162 l1 = __floats2bfloat162_rn(x.z - f1.x, x.w - f1.y);
           const int off = sw128_offset(m, 2 * r2, kTcM);
           *reinterpret_cast<uint2 *>(ahi + off) =
               make_uint2(*reinterpret_cast<uint32_t *>(&h0), *reinterpret_cast<uint32_t *>(&h1));
           *reinterpret_cast<uint2 *>(alo + off) =
               make_uint2(*reinterpret_cast<uint32_t *>(&l0), *reinterpret_cast<uint32_t *>(&l1));
-          part[i] = x[i].x * x[i].x + x[i].y * x[i].y + x[i].z * x[i].z + x[i].w * x[i].w;
+          part[h * HS + i] = x.x * x.x + x.y * x.y + x.z * x.z + x.w * x.w;
         }
+      } else {
+#pragma unroll
+        for (int i = 0; i < HU; i++) {
+          const int j = (p >> 7) + 2 * (h * HU + i);
+          uint32_t hw[4], lw[4];
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            const float2 x = xc[h][i][e];
+            __nv_bfloat162 hb = __floats2bfloat162_rn(x.x, x.y);
+            float2 hf = __bfloat1622float2(hb);
+            __nv_bfloat162 lb = __floats2bfloat162_rn(x.x - hf.x, x.y - hf.y);
+            hw[e] = *reinterpret_cast<uint32_t *>(&hb);
+            lw[e] = *reinterpret_cast<uint32_t *>(&lb);
+            part[0] += x.x * x.x + x.y * x.y;
+          }
+          const int off = sw128_offset(mc, 8 * j, kTcM);
+          *reinterpret_cast<uint4 *>(ahi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          *reinterpret_cast<uint4 *>(alo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+      }
+    };
+    int it = 0;
+    i64 tile = blockIdx.x;
+    if (tile < g.n_tiles) {
+      const i64 base = tile_base(tile, g);
+      load_half(base, 0);
+      load_half(base, 1);
+    }
+    for (; tile < g.n_tiles; tile += gridDim.x, ++it) {
+      const int stage = it & 1;
+      const i64 next = tile + gridDim.x;
+      const bool more = next < g.n_tiles;
+      const i64 nbase = more ? tile_base(next, g) : 0;
+      if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
+      uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
+      uint8_t *alo = ahi + S::A_BYTES;
+      float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
+      part[0] = 0.f;
+      convert_half(0, ahi, alo);
+      if (more) load_half(nbase, 0);
+      convert_half(1, ahi, alo);
+      if (more) load_half(nbase, 1);
+      if constexpr (MODE == kLowMode) {
         // Column norms: part[i] of lane l belongs to the warp's column
         // i * CPS + l / LPC.  A reduce-scatter over the LPC lanes of each
         // column (fixed order, deterministic): after the step with offset o
@@ -360,48 +424,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           sq[kTcM + m] = 0.f;
         }
       } else {
-      const int m = p & (kTcM - 1);
-      const float2 *src = v + base + col_off[m];
-      float2 x[S::UPT][4];
-#pragma unroll
-      for (int i = 0; i < S::UPT; i++) {
-        const int j = (p >> 7) + 2 * i;  // unit: block rows 4j .. 4j+3
-        if constexpr (MODE == kPairMode) {
-          const float4 a = *reinterpret_cast<const float4 *>(src + blk_off[4 * j]);
-          const float4 b = *reinterpret_cast<const float4 *>(src + blk_off[4 * j + 2]);
-          x[i][0] = make_float2(a.x, a.y);
-          x[i][1] = make_float2(a.z, a.w);
-          x[i][2] = make_float2(b.x, b.y);
-          x[i][3] = make_float2(b.z, b.w);
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; e++) x[i][e] = src[blk_off[4 * j + e]];
-        }
-      }
-      if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
-      uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
-      uint8_t *alo = ahi + S::A_BYTES;
-      float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
-      float part_all = 0.f;
-#pragma unroll
-      for (int i = 0; i < S::UPT; i++) {
-        const int j = (p >> 7) + 2 * i;
-        uint32_t h[4], l[4];
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-          __nv_bfloat162 hb = __floats2bfloat162_rn(x[i][e].x, x[i][e].y);
-          float2 hf = __bfloat1622float2(hb);
-          __nv_bfloat162 lb = __floats2bfloat162_rn(x[i][e].x - hf.x, x[i][e].y - hf.y);
-          h[e] = *reinterpret_cast<uint32_t *>(&hb);
-          l[e] = *reinterpret_cast<uint32_t *>(&lb);
-          part_all += x[i][e].x * x[i][e].x + x[i][e].y * x[i][e].y;
-        }
-        const int off = sw128_offset(m, 8 * j, kTcM);
-        *reinterpret_cast<uint4 *>(ahi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4 *>(alo + off) = make_uint4(l[0], l[1], l[2], l[3]);
-      }
-      // threads p and p + 128 hold the two halves of column m's norm
-      sq[(p >> 7) * kTcM + m] = part_all;
+        // threads p and p + 128 hold the two halves of column mc's norm
+        sq[(p >> 7) * kTcM + mc] = part[0];
       }
       fence_async_shared();
       mbar_arrive(bar(stage));
