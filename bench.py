@@ -463,6 +463,8 @@ def run_sweeps(args, dist):
         u6, _ = np.linalg.qr(rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64)))
         u5, _ = np.linalg.qr(rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32)))
         u4, _ = np.linalg.qr(rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16)))
+        u3, _ = np.linalg.qr(rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8)))
+        u2, _ = np.linalg.qr(rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)))
         draws = rng.random(1024)
         Ns = float(s.size) * 8
         ops = {
@@ -474,6 +476,12 @@ def run_sweeps(args, dist):
                        Ns / 2),
             "block_simt4": (lambda i: s.apply_block([(i + 2 * j) % n for j in range(4)], u4,
                                                     capi.FUSE_SIMT), 2 * Ns),
+            "block_simt3": (lambda i: s.apply_block([(i + 2 * j) % n for j in range(3)], u3,
+                                                    capi.FUSE_SIMT), 2 * Ns),
+            "block_simt2": (lambda i: s.apply_block([(i + 2 * j) % n for j in range(2)], u2,
+                                                    capi.FUSE_SIMT), 2 * Ns),
+            "block_auto4": (lambda i: s.apply_block([(i + 2 * j) % n for j in range(4)], u4,
+                                                    capi.FUSE_AUTO), 2 * Ns),
             "block_tc6": (lambda i: s.apply_block([(i + 3 * j) % n for j in range(6)], u6,
                                                   capi.FUSE_TENSOR), 2 * Ns),
             "block_tc5": (lambda i: s.apply_block([(i + 3 * j) % n for j in range(5)], u5,

@@ -193,20 +193,51 @@ static int apply_block_simt_t(qcs_cuda_state *s, int k, const int *qubits, const
   }
 }
 
+// A k-qubit block as a 5-qubit one: the lowest qubits it does not touch are
+// appended as block bits k..4, where the matrix acts as the identity.
+static void widen_to_5(const qcs_cuda_state *s, int k, const int *qubits, const double *u,
+                       int *q5, std::vector<double> &u5) {
+  const int K = 1 << k;
+  int kk = k;
+  for (int j = 0; j < k; j++) q5[j] = qubits[j];
+  for (int q = 0; q < s->n && kk < 5; q++) {
+    bool used = false;
+    for (int j = 0; j < k; j++) used = used || qubits[j] == q;
+    if (!used) q5[kk++] = q;
+  }
+  u5.assign(2 * 32 * 32, 0.0);
+  for (int a = 0; a < 32; a++)
+    for (int b = 0; b < 32; b++)
+      if ((a >> k) == (b >> k)) {
+        const size_t src = 2 * ((size_t)(a & (K - 1)) * K + (b & (K - 1)));
+        u5[2 * (a * 32 + b)] = u[src];
+        u5[2 * (a * 32 + b) + 1] = u[src + 1];
+      }
+}
+
 // Engine choice: the tensor cores take the blocks they support (k = 5, 6 on
-// complex64 states) unless SIMT is asked for; AUTO leaves k <= 4 to the CUDA
-// cores, where the block is bandwidth-bound anyway.  `strict` (explicit
+// complex64 states) unless SIMT is asked for.  AUTO and TENSOR also send
+// 4-qubit blocks to the tensor cores, widened to 5 qubits: on the CUDA cores a
+// 16 x 16 complex product per column is FP32-bound (6.9 ms against 3.4 ms
+// for a 5-qubit tensor-core block at 30 qubits).  `strict` (explicit
 // single-block calls) refuses a TENSOR request the tensor engine cannot
 // serve instead of running it on the CUDA cores.
 int apply_block(qcs_cuda_state *s, int k, const int *qubits, const double *u, int engine,
                 bool strict) {
   invalidate_sum(s);
   const bool tc_ok = tc_supported(s, k);
-  if (engine == QCS_FUSE_TENSOR && strict && !tc_ok)
+  const bool widen = engine != QCS_FUSE_SIMT && k == 4 && tc_supported(s, 5);
+  if (engine == QCS_FUSE_TENSOR && strict && !tc_ok && !widen)
     return set_error(QCS_CUDA_EUNSUP, "tensor-core block engine: unsupported k=%d / precision", k);
   // blocks from the planner (strict == false) are products of unitary gates
   if (tc_ok && (engine == QCS_FUSE_TENSOR || (engine == QCS_FUSE_AUTO && k > 4)))
     return apply_block_tc(s, k, qubits, u, !strict);
+  if (widen) {
+    int q5[5];
+    std::vector<double> u5;
+    widen_to_5(s, k, qubits, u, q5, u5);
+    return apply_block_tc(s, 5, q5, u5.data(), !strict);
+  }
   if (s->prec == QCS_CUDA_C128) return apply_block_simt_t<double2>(s, k, qubits, u);
   return apply_block_simt_t<float2>(s, k, qubits, u);
 }

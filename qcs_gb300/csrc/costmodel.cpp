@@ -72,7 +72,8 @@ int item_category(const qcs_cuda_op *ops, const PlanItem &it, bool tc_ok_5, bool
     if (diag) return CAT_DIAG;
     return CAT_DENSE;
   }
-  if ((k == 5 && tc_ok_5) || (k == 6 && tc_ok_6)) return CAT_TC;
+  // the AUTO engine runs 4-qubit blocks on the tensor cores, widened to 5
+  if ((k == 4 && tc_ok_5) || (k == 5 && tc_ok_5) || (k == 6 && tc_ok_6)) return CAT_TC;
   return CAT_SIMT;
 }
 
@@ -102,7 +103,7 @@ static double grow_cost(int n, int k, int ngates, const int *qubits, void *ctx) 
   const PlanScore &ps = *static_cast<const PlanScore *>(ctx);
   int cat;
   if (k == 1) cat = CAT_DENSE;
-  else if ((k == 5 && ps.tc5) || (k == 6 && ps.tc6)) cat = CAT_TC;
+  else if (((k == 4 || k == 5) && ps.tc5) || (k == 6 && ps.tc6)) cat = CAT_TC;
   else cat = CAT_SIMT;
   float f[kCostFeatures];
   item_features(cat, n, k, ngates, qubits, f);

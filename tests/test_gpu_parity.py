@@ -332,6 +332,35 @@ def test_apply_block_tensor_cores(k, placement):
             assert infidelity(a, b) < 1e-8
 
 
+def test_auto_engine_widens_four_qubit_blocks():
+    """AUTO runs a 4-qubit block on the tensor cores, widened to 5 qubits with
+    the identity on the added qubit; fused circuits at width 4 likewise."""
+    n = 15
+    rng = np.random.default_rng(44)
+    for trial in range(3):
+        qubits = [int(q) for q in rng.choice(n, size=4, replace=False)]
+        m = rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16))
+        u, _ = np.linalg.qr(m)
+        init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        init /= np.linalg.norm(init)
+        with capi.State(n, capi.C64) as s, O.OracleState(n) as o:
+            s.set_amplitudes(init)
+            o.set_amplitudes(init)
+            s.profile(True)
+            s.apply_block(qubits, u, capi.FUSE_AUTO)
+            prof = s.profile_read()
+            s.profile(False)
+            o.apply_block(qubits, u)
+            a, b = s.amplitudes(), o.amplitudes()
+            assert "block_tc" in prof and "block_simt" not in prof
+            assert np.max(np.abs(a - b)) < TC_ATOL
+            assert infidelity(a, b) < 1e-8
+    g = W.brick_circuit(n, 6, 8)
+    with capi.State(n, capi.C64) as s, oracle_state(n, g) as o:
+        s.run(g, fusion_k=4)
+        assert infidelity(s.amplitudes(), o.amplitudes()) < 1e-6
+
+
 def test_tensor_cores_preserve_the_norm_over_many_blocks():
     """100 random 6-qubit unitaries: FP32 accumulation in the tensor cores
     rounds toward zero; the per-column norm restore must keep the state's
