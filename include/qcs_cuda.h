@@ -242,8 +242,10 @@ int qcs_cuda_batch_config(qcs_cuda_batch *b, int threads, int tile_q,
  * An MLP (QCS_COSTMODEL_FEATURES inputs, three hidden layers of 64 ReLU
  * units, one output) that predicts log2 of a plan item's device time in ms.
  * Forward, backward and Adam run on the GPU in this library's own kernels;
- * the host keeps a copy of the weights for planning.  No reference
- * counterpart (the reference has no fusion). */
+ * the host keeps a copy of the weights for planning.  Created where no
+ * device is visible, a model serves planning only: get/set_params,
+ * predict_host and plan_learned work, training and predict return
+ * QCS_CUDA_ENODEV.  No reference counterpart (the reference has no fusion). */
 #define QCS_COSTMODEL_FEATURES 20
 typedef struct qcs_cuda_costmodel qcs_cuda_costmodel;
 int qcs_cuda_costmodel_create(int num_features, unsigned long long seed,

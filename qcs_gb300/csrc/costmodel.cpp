@@ -210,10 +210,8 @@ std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n
       refined.push_back(std::move(it));
     }
   }
-  if (splits) {
-    best = std::move(refined);
-    best_ms = plan_ms(ps, best);
-  }
+  best = std::move(refined);  // every item was moved into `refined`
+  if (splits) best_ms = plan_ms(ps, best);
   if (pred_ms) *pred_ms = best_ms;
   if (greedy_ms) *greedy_ms = judge;
   if (choice) *choice = best_choice + 1000 * splits;

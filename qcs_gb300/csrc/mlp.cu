@@ -188,6 +188,7 @@ struct qcs_cuda_costmodel {
   int step;
   std::vector<float> host_params;  // mirror for planning on the host
   unsigned long long generation;   // bumped whenever host_params change
+  bool host_only;                  // no device: host planning only
   cudaStream_t stream;
 };
 
@@ -288,27 +289,29 @@ int qcs_cuda_costmodel_create(int num_features, unsigned long long seed, qcs_cud
     return set_error(QCS_CUDA_EINVAL, "cost model: 1..64 features");
   *out = nullptr;
   int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-    cudaGetLastError();
-    return set_error(QCS_CUDA_ENODEV, "no CUDA device visible");
-  }
+  const bool host_only = cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0;
+  if (host_only) cudaGetLastError();
   qcs_cuda_costmodel *m = new qcs_cuda_costmodel();
   m->F = num_features;
   m->count = MlpShape(num_features).count;
-  int rc = check_cuda(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-  const size_t pb = (size_t)m->count * sizeof(float);
-  if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_params, pb), "cudaMalloc(mlp)");
-  if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_grad, pb), "cudaMalloc(mlp)");
-  if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_m, pb), "cudaMalloc(mlp)");
-  if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_v, pb), "cudaMalloc(mlp)");
-  if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_loss, sizeof(double)), "cudaMalloc(mlp)");
-  if (!rc)
-    rc = check_cuda(cudaFuncSetAttribute(k_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)mlp_smem(64)),
-                    "cudaFuncSetAttribute(mlp)");
-  if (rc) {
-    qcs_cuda_costmodel_destroy(m);
-    return rc;
+  m->host_only = host_only;
+  int rc = QCS_CUDA_OK;
+  if (!host_only) {
+    rc = check_cuda(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    const size_t pb = (size_t)m->count * sizeof(float);
+    if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_params, pb), "cudaMalloc(mlp)");
+    if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_grad, pb), "cudaMalloc(mlp)");
+    if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_m, pb), "cudaMalloc(mlp)");
+    if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_v, pb), "cudaMalloc(mlp)");
+    if (!rc) rc = check_cuda(cudaMalloc((void **)&m->d_loss, sizeof(double)), "cudaMalloc(mlp)");
+    if (!rc)
+      rc = check_cuda(cudaFuncSetAttribute(k_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)mlp_smem(64)),
+                      "cudaFuncSetAttribute(mlp)");
+    if (rc) {
+      qcs_cuda_costmodel_destroy(m);
+      return rc;
+    }
   }
   // He initialisation from a splitmix64 stream (host), biases zero
   std::vector<float> p(m->count, 0.f);
@@ -346,6 +349,10 @@ int qcs_cuda_costmodel_create(int num_features, unsigned long long seed, qcs_cud
 
 int qcs_cuda_costmodel_destroy(qcs_cuda_costmodel *m) {
   if (!m) return set_error(QCS_CUDA_EINVAL, "null model");
+  if (m->host_only) {
+    delete m;
+    return QCS_CUDA_OK;
+  }
   if (m->stream) cudaStreamSynchronize(m->stream);
   cudaFree(m->d_params);
   cudaFree(m->d_grad);
@@ -370,13 +377,18 @@ int qcs_cuda_costmodel_num_params(qcs_cuda_costmodel *m, int *count) {
 
 int qcs_cuda_costmodel_get_params(qcs_cuda_costmodel *m, float *out) {
   if (!m || !out) return set_error(QCS_CUDA_EINVAL, "null argument");
-  int rc = cm_sync_host(m);
+  int rc = m->host_only ? QCS_CUDA_OK : cm_sync_host(m);
   if (!rc) memcpy(out, m->host_params.data(), m->count * sizeof(float));
   return rc;
 }
 
 int qcs_cuda_costmodel_set_params(qcs_cuda_costmodel *m, const float *in, int count) {
   if (!m || !in || count != m->count) return set_error(QCS_CUDA_EINVAL, "bad parameter vector");
+  if (m->host_only) {
+    m->host_params.assign(in, in + count);
+    m->generation = ++g_cm_generation;
+    return QCS_CUDA_OK;
+  }
   int rc = check_cuda(cudaMemcpyAsync(m->d_params, in, count * sizeof(float), cudaMemcpyHostToDevice,
                                       m->stream),
                       "cost model params");
@@ -389,6 +401,7 @@ int qcs_cuda_costmodel_set_params(qcs_cuda_costmodel *m, const float *in, int co
 int qcs_cuda_costmodel_loss_grad(qcs_cuda_costmodel *m, const float *x, const float *y, int n,
                                  double *loss, float *grad) {
   if (!m || !x || !y || n < 1) return set_error(QCS_CUDA_EINVAL, "bad arguments");
+  if (m->host_only) return set_error(QCS_CUDA_ENODEV, "cost model without a device: planning only");
   int rc = cm_reserve(m, n);
   if (!rc) rc = check_cuda(cudaMemcpyAsync(m->d_x, x, (size_t)n * m->F * 4, cudaMemcpyHostToDevice, m->stream), "upload");
   if (!rc) rc = check_cuda(cudaMemcpyAsync(m->d_y, y, (size_t)n * 4, cudaMemcpyHostToDevice, m->stream), "upload");
@@ -405,6 +418,7 @@ int qcs_cuda_costmodel_loss_grad(qcs_cuda_costmodel *m, const float *x, const fl
 int qcs_cuda_costmodel_train(qcs_cuda_costmodel *m, const float *x, const float *y, int n,
                              int epochs, int batch, float lr, double *final_loss) {
   if (!m || !x || !y || n < 1 || epochs < 1 || batch < 1) return set_error(QCS_CUDA_EINVAL, "bad arguments");
+  if (m->host_only) return set_error(QCS_CUDA_ENODEV, "cost model without a device: planning only");
   if (batch > n) batch = n;
   int rc = cm_reserve(m, n);
   if (!rc) rc = check_cuda(cudaMemcpyAsync(m->d_x, x, (size_t)n * m->F * 4, cudaMemcpyHostToDevice, m->stream), "upload");
@@ -429,6 +443,7 @@ int qcs_cuda_costmodel_train(qcs_cuda_costmodel *m, const float *x, const float 
 
 int qcs_cuda_costmodel_predict(qcs_cuda_costmodel *m, const float *x, int n, float *out) {
   if (!m || !x || !out || n < 1) return set_error(QCS_CUDA_EINVAL, "bad arguments");
+  if (m->host_only) return set_error(QCS_CUDA_ENODEV, "cost model without a device: planning only");
   int rc = cm_reserve(m, n);
   if (!rc) rc = check_cuda(cudaMemcpyAsync(m->d_x, x, (size_t)n * m->F * 4, cudaMemcpyHostToDevice, m->stream), "upload");
   if (rc) return rc;
