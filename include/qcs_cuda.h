@@ -292,8 +292,7 @@ int qcs_cuda_state_set_costmodel(qcs_cuda_state *s, qcs_cuda_costmodel *m);
  * qcs_cuda_plan), the model's predicted ms for it and for the greedy
  * width-kmax plan, and which candidate won (2..7: greedy width; 100 + k:
  * model-stopped growth at width k), plus 1000 x the number of that
- * candidate's blocks the model then split into narrower items or widened
- * onto the tensor cores. */
+ * candidate's blocks the model then split into narrower items. */
 int qcs_cuda_plan_learned(const qcs_cuda_op *ops, int count, int num_qubits,
                           int kmax, qcs_cuda_costmodel *m, int *order,
                           int *item, int *num_items, double *pred_ms,

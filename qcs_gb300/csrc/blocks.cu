@@ -217,16 +217,16 @@ static void widen_to_5(const qcs_cuda_state *s, int k, const int *qubits, const 
 
 // Engine choice: the tensor cores take the blocks they support (k = 5, 6 on
 // complex64 states) unless SIMT is asked for.  AUTO and TENSOR also send
-// 4-qubit blocks to the tensor cores, widened to 5 qubits: on the CUDA cores a
-// 16 x 16 complex product per column is FP32-bound (6.9 ms against 3.4 ms
-// for a 5-qubit tensor-core block at 30 qubits).  `strict` (explicit
+// 2..4-qubit blocks to the tensor cores, widened to 5 qubits: at 30 qubits
+// the CUDA-core kernel takes 6.3 / 5.8 / 6.9 ms for k = 2 / 3 / 4 against
+// 3.0 ms for a 5-qubit tensor-core block.  `strict` (explicit
 // single-block calls) refuses a TENSOR request the tensor engine cannot
 // serve instead of running it on the CUDA cores.
 int apply_block(qcs_cuda_state *s, int k, const int *qubits, const double *u, int engine,
                 bool strict) {
   invalidate_sum(s);
   const bool tc_ok = tc_supported(s, k);
-  const bool widen = engine != QCS_FUSE_SIMT && k == 4 && tc_supported(s, 5);
+  const bool widen = engine != QCS_FUSE_SIMT && k >= 2 && k <= 4 && tc_supported(s, 5);
   if (engine == QCS_FUSE_TENSOR && strict && !tc_ok && !widen)
     return set_error(QCS_CUDA_EUNSUP, "tensor-core block engine: unsupported k=%d / precision", k);
   // blocks from the planner (strict == false) are products of unitary gates

@@ -61,7 +61,7 @@ constexpr int kTcEpiThreads = kTcEpiWarps * 32;          // 128
 constexpr long long kWaitCycles = 4000000000LL;          // ~2 s at 2 GHz
 constexpr int kImgSlots = 8;                             // block-matrix upload ring
 constexpr int kSqSlots = 4;                              // column-norm ring
-constexpr int kEpiPitch = 33;  // floats per staged column (conflict-free transpose)
+constexpr int kEpiPitch = 34;  // floats per staged column (even: 8-byte accesses, 2 wavefronts)
 
 // Memory access modes of the kernel (chosen per block on the host):
 //   kColMode   qubit 0 is a column qubit: a warp's 32 columns are adjacent
@@ -498,18 +498,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         // Result block c of this warp: 32 columns x 32 reals (rows 16c ..
         // 16c+15), transposed through shared memory so that each store
         // instruction writes one column's 16 adjacent amplitudes (128 B).
+        // Staged as float2: lane m writes its column's 16 amplitudes in row m;
+        // then lanes 0-15 store column j and lanes 16-31 column j+1, one
+        // amplitude each, two full 128-byte lines per instruction.
         float *buf = epi + warp * 32 * kEpiPitch;
+        const int half = lane >> 4, row = lane & 15;
 #pragma unroll 1
         for (int c = 0; c < S::N / 32; c++) {
           float acc[32];
           tmem_ld32(tb + 32 * c, acc);
 #pragma unroll
-          for (int q = 0; q < 32; q++) buf[lane * kEpiPitch + q] = acc[q] * scale;
+          for (int q = 0; q < 16; q++)
+            *reinterpret_cast<float2 *>(buf + lane * kEpiPitch + 2 * q) =
+                make_float2(acc[2 * q] * scale, acc[2 * q + 1] * scale);
           __syncwarp();
 #pragma unroll 4
-          for (int j = 0; j < 32; j++) {
-            float *col = reinterpret_cast<float *>(v + base + col_off[warp * 32 + j] + 16 * c);
-            col[lane] = buf[j * kEpiPitch + lane];
+          for (int j = 0; j < 32; j += 2) {
+            const float2 val = *reinterpret_cast<const float2 *>(buf + (j + half) * kEpiPitch + 2 * row);
+            v[base + col_off[warp * 32 + j + half] + 16 * c + row] = val;
           }
           __syncwarp();
         }

@@ -72,8 +72,8 @@ int item_category(const qcs_cuda_op *ops, const PlanItem &it, bool tc_ok_5, bool
     if (diag) return CAT_DIAG;
     return CAT_DENSE;
   }
-  // the AUTO engine runs 4-qubit blocks on the tensor cores, widened to 5
-  if ((k == 4 && tc_ok_5) || (k == 5 && tc_ok_5) || (k == 6 && tc_ok_6)) return CAT_TC;
+  // AUTO runs 2..4-qubit blocks on the tensor cores, widened to 5 qubits
+  if ((k >= 2 && k <= 5 && tc_ok_5) || (k == 6 && tc_ok_6)) return CAT_TC;
   return CAT_SIMT;
 }
 
@@ -103,17 +103,16 @@ static double grow_cost(int n, int k, int ngates, const int *qubits, void *ctx) 
   const PlanScore &ps = *static_cast<const PlanScore *>(ctx);
   int cat;
   if (k == 1) cat = CAT_DENSE;
-  else if (((k == 4 || k == 5) && ps.tc5) || (k == 6 && ps.tc6)) cat = CAT_TC;
+  else if ((k >= 2 && k <= 5 && ps.tc5) || (k == 6 && ps.tc6)) cat = CAT_TC;
   else cat = CAT_SIMT;
   float f[kCostFeatures];
   item_features(cat, n, k, ngates, qubits, f);
   return exp2((double)costmodel_predict_host(ps.m, f));
 }
 
-// Cheapest predicted way to run one block's gates: the block itself, its
+// Cheapest predicted way to run one block's gates: the block itself, or its
 // gates re-partitioned greedily at every narrower width (width 1: every gate
-// on its own, or merged with same-qubit neighbours), or the block widened to
-// five qubits for the tensor cores.  The block's gate order is a valid execution order of those
+// on its own, or merged with same-qubit neighbours).  The block's gate order is a valid execution order of those
 // gates, so each alternative may replace the block in place.  Returns true
 // (and fills *out) when an alternative is predicted faster.
 static bool refine_block(const PlanScore &ps, const PlanItem &it, std::vector<PlanItem> *out) {
@@ -141,22 +140,6 @@ static bool refine_block(const PlanScore &ps, const PlanItem &it, std::vector<Pl
     if (t < best) {
       best = t;
       best_items = std::move(cand);
-    }
-  }
-  // Widened onto the tensor cores: a block of k < 5 qubits padded with the
-  // lowest qubits it does not touch (identity there) runs as a 5-qubit
-  // tensor-core block instead of a CUDA-core one.
-  if (ps.tc5 && k < 5 && ps.n >= 5) {
-    PlanItem wide = it;
-    for (int j = 0; j < m; j++) wide.gates[j] = j;
-    for (int q = 0; q < ps.n && (int)wide.qubits.size() < 5; q++)
-      if (std::find(it.qubits.begin(), it.qubits.end(), q) == it.qubits.end())
-        wide.qubits.push_back(q);
-    std::sort(wide.qubits.begin(), wide.qubits.end());
-    const double t = item_ms(sps, wide);
-    if (t < best) {
-      best = t;
-      best_items.assign(1, std::move(wide));
     }
   }
   if (best_items.empty()) return false;
@@ -196,8 +179,7 @@ std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n
     }
   }
   // Block by block: split the blocks the model predicts slower than their
-  // parts (a wide block holding a few diagonal gates, say), or widen the
-  // narrow ones it predicts faster on the tensor cores.
+  // parts (a wide block holding a few diagonal gates, say).
   std::vector<PlanItem> refined;
   refined.reserve(best.size());
   int splits = 0;
