@@ -104,10 +104,16 @@ struct TcShape {
 struct TcGeom {
   i64 n_tiles;
   int nfree;
+  int nruns;          // contiguous runs of a tile (at most 64)
+  int run_bytes;      // bytes per run (>= 1 KB: the tile holds qubits 0..6)
   signed char freeq[40];
   i64 col_off[kTcM];  // column m -> offset (bits of m on the column qubits)
   i64 blk_off[64];    // block index a -> offset (bit j of a on qubits[j])
+  i64 run_off[64];    // run j -> offset of its first amplitude
 };
+
+// Tiles ahead of the one being converted whose runs are prefetched into L2.
+constexpr int kPrefetchAhead = 2;
 
 // Byte offset of bf16 element (r, k) in a K-major operand of R rows laid out
 // in 128-byte swizzle atoms (8 rows x 64 elements, 16-byte chunks permuted by
@@ -120,6 +126,11 @@ __host__ __device__ __forceinline__ int sw128_offset(int r, int k, int R) {
 // ---- PTX wrappers ---------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
+}
+// Bulk prefetch of [p, p + bytes) into L2 (p 16-byte aligned, bytes a
+// multiple of 16); no destination, no completion to wait for.
+__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
@@ -386,6 +397,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const i64 next = tile + gridDim.x;
       const bool more = next < g.n_tiles;
       const i64 nbase = more ? tile_base(next, g) : 0;
+      // the runs of the tile kPrefetchAhead ahead go to L2 now, so that the
+      // register loads issued for the next tile below find them there
+      {
+        const i64 far = tile + (i64)kPrefetchAhead * gridDim.x;
+        if (p < g.nruns && far < g.n_tiles)
+          prefetch_l2(v + tile_base(far, g) + g.run_off[p], (uint32_t)g.run_bytes);
+      }
       if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
       uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
       uint8_t *alo = ahi + S::A_BYTES;
@@ -728,6 +746,24 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
     for (int j = 0; j < k; j++)
       if ((a >> j) & 1) o |= 1LL << qubits[j];
     g.blk_off[a] = o;
+  }
+  {
+    // the tile's qubits ascending; the lowest R of them are 0..R-1 (R >= 7),
+    // so the tile is 2^(k+7-R) runs of 2^R adjacent amplitudes
+    std::vector<int> tq;
+    for (int q = 0; q < s->n; q++)
+      if (role[q] != -1) tq.push_back(q);
+    int R = 0;
+    while (R < (int)tq.size() && tq[R] == R) R++;
+    const int nt = (int)tq.size();
+    g.nruns = 1 << (nt - R);
+    g.run_bytes = (int)(8LL << R);
+    for (int j = 0; j < g.nruns; j++) {
+      i64 o = 0;
+      for (int b = R; b < nt; b++)
+        if ((j >> (b - R)) & 1) o |= 1LL << tq[b];
+      g.run_off[j] = o;
+    }
   }
   bool low = true;  // the block is exactly qubits 0..k-1
   for (int j = 0; j < k; j++) low = low && qubits[j] == j;
