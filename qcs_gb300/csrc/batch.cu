@@ -9,8 +9,13 @@
 //  * CTAs pull instances from an atomic queue, largest first (the order is
 //    part of the tuned schedule);
 //  * an instance of at most `tile_q` qubits lives entirely in shared memory:
-//    |0...0> is built there, every gate is one pass over shared memory, and
-//    <Z_0> and the shots are computed there -- it never touches HBM;
+//    |0...0> is built there, its gates run there, and <Z_0> and the shots
+//    are computed there -- it never touches HBM;
+//  * gates run in register groups: the gates of a stage are partitioned
+//    greedily into groups on at most 4 tile bits, and one pass over shared
+//    memory applies a whole group, each thread holding the 16 amplitudes of
+//    one setting of the other bits in registers (one pass per group instead
+//    of one per gate);
 //  * a larger instance lives in a per-CTA slot of global memory and runs in
 //    stages: a stage is a set of tile_q qubits and the gates acting inside
 //    it; for every tile (one setting of the other qubits) the CTA gathers the
@@ -47,16 +52,27 @@ struct BInst {
 };
 
 struct BStage {
-  int gate0;
-  int ngates;
+  int group0;
+  int ngroups;
   int nt;             // tile qubits (local bits)
   int pad;
   signed char q[24];  // local bit m -> global qubit (ascending)
 };
 
+// Up to kGroupQ tile bits whose gates run in one pass: each thread holds the
+// 2^r amplitudes of one setting of the other bits in registers and applies
+// the group's gates to them in order.
+constexpr int kGroupQ = 4;
+struct BGroup {
+  int gate0;
+  int ngates;
+  int r;                    // group bits
+  signed char q[kGroupQ];   // tile bit of group bit j (ascending)
+};
+
 struct BGate {
   float2 m[4];
-  int type;  // 0: 2x2 on bit t; 1: 2x2 on bit t where bit c is set
+  int type;  // 0: 2x2 on group bit t; 1: 2x2 on group bit t where bit c is set
   int t, c;
   int pad;
 };
@@ -81,7 +97,9 @@ struct qcs_cuda_batch {
   // plan (for the current tile size)
   std::vector<qcs::BInst> insts;
   std::vector<qcs::BStage> stages;
-  std::vector<int> gate_op;       // op index of every planned gate
+  std::vector<qcs::BGroup> groups;
+  std::vector<int> gate_op;       // op index of every planned gate (group order)
+  std::vector<int> gate_tc;       // its group-local target | control << 8 (control 0xFF: none)
   std::vector<int> order;
   qcs::BatchTune tune;
   int planned_tile_q;
@@ -90,6 +108,7 @@ struct qcs_cuda_batch {
   qcs::DeviceInfo dev;
   qcs::BInst *d_insts;
   qcs::BStage *d_stages;
+  qcs::BGroup *d_groups;
   qcs::BGate *d_gates;
   qcs::BGate *h_gates;  // pinned; the graph's upload node reads it
   int *d_order;
@@ -149,31 +168,66 @@ __device__ double block_sum(double v, double *red) {
   return r;  // valid in thread 0
 }
 
-// Apply one gate to a tile of 2^nt amplitudes in shared memory.
+// One 2x2 on register bit TB of the R amplitudes a[] (controlled: only where
+// register bit c is set).  Static indices keep a[] in registers.
+template <int R, int TB>
+__device__ __forceinline__ void reg_gate(float2 (&a)[1 << kGroupQ], const BGate &g) {
+#pragma unroll
+  for (int e = 0; e < R; e++) {
+    if (e & (1 << TB)) continue;
+    if (g.type && !((e >> g.c) & 1)) continue;
+    const float2 v0 = a[e], v1 = a[e | (1 << TB)];
+    a[e] = cadd(cmul(g.m[0], v0), cmul(g.m[1], v1));
+    a[e | (1 << TB)] = cadd(cmul(g.m[2], v0), cmul(g.m[3], v1));
+  }
+}
+
+// Apply one group to a tile of 2^nt amplitudes in shared memory.
+template <int T, int RB>
+__device__ __forceinline__ void smem_group_r(float2 *S, int nt, const BGroup &G,
+                                             const BGate *gates) {
+  constexpr int R = 1 << RB;
+  const int np = 1 << (nt - RB);
+  int qb[kGroupQ];
+#pragma unroll
+  for (int j = 0; j < RB; j++) qb[j] = G.q[j];
+  for (int p = threadIdx.x; p < np; p += T) {
+    int base = p;
+#pragma unroll
+    for (int j = 0; j < RB; j++)  // ascending: insert a zero at tile bit qb[j]
+      base = ((base >> qb[j]) << (qb[j] + 1)) | (base & ((1 << qb[j]) - 1));
+    // offset of register e: base with group bit j of e at tile bit qb[j]
+    auto off = [&](int e) {
+      int o = base;
+#pragma unroll
+      for (int j = 0; j < RB; j++)
+        if ((e >> j) & 1) o |= 1 << qb[j];
+      return o;
+    };
+    float2 a[1 << kGroupQ];
+#pragma unroll
+    for (int e = 0; e < R; e++) a[e] = S[off(e)];
+    for (int gi = 0; gi < G.ngates; gi++) {
+      const BGate g = gates[G.gate0 + gi];
+      switch (g.t) {
+        case 0: reg_gate<R, 0>(a, g); break;
+        case 1: if constexpr (RB > 1) reg_gate<R, 1>(a, g); break;
+        case 2: if constexpr (RB > 2) reg_gate<R, 2>(a, g); break;
+        default: if constexpr (RB > 3) reg_gate<R, 3>(a, g); break;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < R; e++) S[off(e)] = a[e];
+  }
+}
+
 template <int T>
-__device__ __forceinline__ void smem_gate(float2 *S, int nt, const BGate &g) {
-  const int t = g.t;
-  const int tb = 1 << t;
-  if (g.type == 0) {
-    const int np = 1 << (nt - 1);
-    for (int p = threadIdx.x; p < np; p += T) {
-      const int lo = ((p >> t) << (t + 1)) | (p & (tb - 1));
-      const float2 v0 = S[lo], v1 = S[lo + tb];
-      S[lo] = cadd(cmul(g.m[0], v0), cmul(g.m[1], v1));
-      S[lo + tb] = cadd(cmul(g.m[2], v0), cmul(g.m[3], v1));
-    }
-  } else {
-    const int c = g.c;
-    const int blo = c < t ? c : t, bhi = c < t ? t : c;
-    const int np = 1 << (nt - 2);
-    for (int p = threadIdx.x; p < np; p += T) {
-      int x = ((p >> blo) << (blo + 1)) | (p & ((1 << blo) - 1));
-      x = ((x >> bhi) << (bhi + 1)) | (x & ((1 << bhi) - 1));
-      const int lo = x | (1 << c);
-      const float2 v0 = S[lo], v1 = S[lo + tb];
-      S[lo] = cadd(cmul(g.m[0], v0), cmul(g.m[1], v1));
-      S[lo + tb] = cadd(cmul(g.m[2], v0), cmul(g.m[3], v1));
-    }
+__device__ __forceinline__ void smem_group(float2 *S, int nt, const BGroup &G, const BGate *gates) {
+  switch (G.r) {
+    case 1: smem_group_r<T, 1>(S, nt, G, gates); break;
+    case 2: smem_group_r<T, 2>(S, nt, G, gates); break;
+    case 3: smem_group_r<T, 3>(S, nt, G, gates); break;
+    default: smem_group_r<T, 4>(S, nt, G, gates); break;
   }
 }
 
@@ -235,9 +289,11 @@ __device__ void smem_prefix(double *x, int m) {
   __syncthreads();
 }
 
+// 64 registers a thread: two CTAs of 512 threads (or one of 1024) fit an SM.
 template <int T>
-__global__ void __launch_bounds__(T)
-    k_batch(const BInst *insts, const BStage *stages, const BGate *gates, const int *order,
+__global__ void __launch_bounds__(T, 1024 / T)
+    k_batch(const BInst *insts, const BStage *stages, const BGroup *groups, const BGate *gates,
+            const int *order,
             int count, int shots, u64 seed, int tile_q, float2 *slots, i64 slot_amps,
             int *queue, double *z_out, i64 *samples_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -265,8 +321,8 @@ __global__ void __launch_bounds__(T)
       for (int i = threadIdx.x; i < L; i += T) S[i] = make_float2(i == 0 ? 1.f : 0.f, 0.f);
       __syncthreads();
       const BStage st = stages[I.stage0];
-      for (int gi = 0; gi < st.ngates; gi++) {
-        smem_gate<T>(S, I.n, gates[st.gate0 + gi]);
+      for (int gi = 0; gi < st.ngroups; gi++) {
+        smem_group<T>(S, I.n, groups[st.group0 + gi], gates);
         __syncthreads();
       }
       const int tile = L < kMassTile ? L : kMassTile;
@@ -333,8 +389,8 @@ __global__ void __launch_bounds__(T)
             S[l] = si == 0 ? make_float2(gidx == 0 ? 1.f : 0.f, 0.f) : slot[gidx];
           }
           __syncthreads();
-          for (int gi = 0; gi < st.ngates; gi++) {
-            smem_gate<T>(S, nt, gates[st.gate0 + gi]);
+          for (int gi = 0; gi < st.ngroups; gi++) {
+            smem_group<T>(S, nt, groups[st.group0 + gi], gates);
             __syncthreads();
           }
           for (int l = threadIdx.x; l < L; l += T) slot[base + goff_lo[l & 63] + goff_hi[l >> 6]] = S[l];
@@ -375,10 +431,54 @@ __global__ void __launch_bounds__(T)
 // host side
 // ---------------------------------------------------------------------------
 
+// The gates of one stage (op indices in order) on tile qubits tq (ascending)
+// as register groups of at most kGroupQ tile bits: a greedy partition of the
+// stage's gates (commuting only past gates on disjoint qubits).
+static void plan_groups(qcs_cuda_batch *b, const std::vector<int> &stage_ops, int n,
+                        const std::vector<int> &tq, BStage &st) {
+  st.group0 = (int)b->groups.size();
+  std::vector<qcs_cuda_op> sub(stage_ops.size());
+  for (size_t j = 0; j < stage_ops.size(); j++) sub[j] = b->ops[stage_ops[j]];
+  PartitionOptions po;
+  po.kmax = kGroupQ;
+  po.cost = nullptr;
+  po.cost_ctx = nullptr;
+  std::vector<PlanItem> items = partition(sub.data(), (int)sub.size(), n, po);
+  auto tile_bit = [&](int q) {
+    for (size_t m = 0; m < tq.size(); m++)
+      if (tq[m] == q) return (int)m;
+    return -1;
+  };
+  for (const PlanItem &it : items) {
+    BGroup G;
+    memset(&G, 0, sizeof(G));
+    G.gate0 = (int)b->gate_op.size();
+    G.r = (int)it.qubits.size();
+    for (int j = 0; j < G.r; j++) G.q[j] = (signed char)tile_bit(it.qubits[j]);
+    auto group_bit = [&](int q) {
+      for (int j = 0; j < G.r; j++)
+        if (it.qubits[j] == q) return j;
+      return -1;
+    };
+    for (int g : it.gates) {
+      const qcs_cuda_op &o = sub[g];
+      const int t = group_bit(o.target);
+      const int c = gate_is_controlled(o.kind) ? group_bit(o.control) : 0xFF;
+      b->gate_op.push_back(stage_ops[g]);
+      b->gate_tc.push_back(t | (c << 8));
+    }
+    G.ngates = (int)b->gate_op.size() - G.gate0;
+    b->groups.push_back(G);
+  }
+  st.ngroups = (int)b->groups.size() - st.group0;
+}
+
 static int batch_plan(qcs_cuda_batch *b, int tile_q) {
   b->insts.clear();
   b->stages.clear();
+  b->groups.clear();
   b->gate_op.clear();
+  b->gate_tc.clear();
   for (int i = 0; i < b->count; i++) {
     BInst I;
     I.n = b->nq[i];
@@ -386,27 +486,15 @@ static int batch_plan(qcs_cuda_batch *b, int tile_q) {
     I.shots_off = 0;
     const qcs_cuda_op *ops = b->ops.data() + b->op_off[i];
     const int nops = b->op_off[i + 1] - b->op_off[i];
-    auto add_gate = [&](int op_index, const std::vector<int> &tq) {
-      const qcs_cuda_op &o = b->ops[op_index];
-      auto local = [&](int q) {
-        for (size_t m = 0; m < tq.size(); m++)
-          if (tq[m] == q) return (int)m;
-        return -1;
-      };
-      b->gate_op.push_back(op_index);
-      (void)o;
-      (void)local;
-    };
     if (I.n <= tile_q) {
       BStage st;
       memset(&st, 0, sizeof(st));
-      st.gate0 = (int)b->gate_op.size();
       st.nt = I.n;
-      std::vector<int> tq(I.n);
+      std::vector<int> tq(I.n), stage_ops(nops);
       std::iota(tq.begin(), tq.end(), 0);
+      std::iota(stage_ops.begin(), stage_ops.end(), b->op_off[i]);
       for (int m = 0; m < I.n; m++) st.q[m] = (signed char)m;
-      for (int j = 0; j < nops; j++) add_gate(b->op_off[i] + j, tq);
-      st.ngates = (int)b->gate_op.size() - st.gate0;
+      plan_groups(b, stage_ops, I.n, tq, st);
       b->stages.push_back(st);
       I.nstages = 1;
     } else {
@@ -424,7 +512,6 @@ static int batch_plan(qcs_cuda_batch *b, int tile_q) {
       for (const PlanItem &it : plan) {
         BStage st;
         memset(&st, 0, sizeof(st));
-        st.gate0 = (int)b->gate_op.size();
         std::vector<char> in(I.n, 0);
         for (int q : it.qubits) in[q] = 1;
         int cnt = (int)it.qubits.size();
@@ -438,8 +525,9 @@ static int batch_plan(qcs_cuda_batch *b, int tile_q) {
           if (in[q]) tq.push_back(q);
         st.nt = (int)tq.size();
         for (int m = 0; m < st.nt; m++) st.q[m] = (signed char)tq[m];
-        for (int g : it.gates) add_gate(b->op_off[i] + g, tq);
-        st.ngates = (int)b->gate_op.size() - st.gate0;
+        std::vector<int> stage_ops;
+        for (int g : it.gates) stage_ops.push_back(b->op_off[i] + g);
+        plan_groups(b, stage_ops, I.n, tq, st);
         b->stages.push_back(st);
       }
       I.nstages = (int)plan.size();
@@ -450,31 +538,19 @@ static int batch_plan(qcs_cuda_batch *b, int tile_q) {
   return QCS_CUDA_OK;
 }
 
-// Gate table from the ops and the current angles (local bit positions).
+// Gate table from the ops and the current angles (group-local bits).
 static void batch_fill_gates(qcs_cuda_batch *b) {
-  size_t gi = 0;
-  for (int i = 0; i < b->count; i++) {
-    const BInst &I = b->insts[i];
-    for (int s = 0; s < I.nstages; s++) {
-      const BStage &st = b->stages[I.stage0 + s];
-      for (int k = 0; k < st.ngates; k++, gi++) {
-        const qcs_cuda_op &o = b->ops[b->gate_op[st.gate0 + k]];
-        double m[8];
-        gate_matrix(o.kind, o.angle, m);
-        BGate g;
-        memset(&g, 0, sizeof(g));
-        for (int e = 0; e < 4; e++) g.m[e] = make_float2((float)m[2 * e], (float)m[2 * e + 1]);
-        auto local = [&](int q) {
-          for (int mm = 0; mm < st.nt; mm++)
-            if (st.q[mm] == q) return mm;
-          return -1;
-        };
-        g.type = gate_is_controlled(o.kind) ? 1 : 0;
-        g.t = local(o.target);
-        g.c = g.type ? local(o.control) : 0;
-        b->h_gates[st.gate0 + k] = g;
-      }
-    }
+  for (size_t gi = 0; gi < b->gate_op.size(); gi++) {
+    const qcs_cuda_op &o = b->ops[b->gate_op[gi]];
+    double m[8];
+    gate_matrix(o.kind, o.angle, m);
+    BGate g;
+    memset(&g, 0, sizeof(g));
+    for (int e = 0; e < 4; e++) g.m[e] = make_float2((float)m[2 * e], (float)m[2 * e + 1]);
+    g.type = gate_is_controlled(o.kind) ? 1 : 0;
+    g.t = b->gate_tc[gi] & 0xFF;
+    g.c = g.type ? (b->gate_tc[gi] >> 8) & 0xFF : 0;
+    b->h_gates[gi] = g;
   }
 }
 
@@ -483,11 +559,13 @@ static void batch_free_device(qcs_cuda_batch *b) {
   b->graph = nullptr;
   cudaFree(b->d_insts);
   cudaFree(b->d_stages);
+  cudaFree(b->d_groups);
   cudaFree(b->d_gates);
   if (b->h_gates) cudaFreeHost(b->h_gates);
   cudaFree(b->d_order);
   b->d_insts = nullptr;
   b->d_stages = nullptr;
+  b->d_groups = nullptr;
   b->d_gates = nullptr;
   b->h_gates = nullptr;
   b->d_order = nullptr;
@@ -506,6 +584,7 @@ static int batch_upload(qcs_cuda_batch *b) {
   batch_free_device(b);
   int rc = check_cuda(cudaMalloc((void **)&b->d_insts, b->insts.size() * sizeof(BInst)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_stages, b->stages.size() * sizeof(BStage)), "cudaMalloc(batch)");
+  if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_groups, std::max<size_t>(1, b->groups.size()) * sizeof(BGroup)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_gates, std::max<size_t>(1, b->gate_op.size()) * sizeof(BGate)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMallocHost((void **)&b->h_gates, std::max<size_t>(1, b->gate_op.size()) * sizeof(BGate)), "cudaMallocHost(batch)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_order, b->count * sizeof(int)), "cudaMalloc(batch)");
@@ -523,6 +602,7 @@ static int batch_upload(qcs_cuda_batch *b) {
   }
   rc = check_cuda(cudaMemcpy(b->d_insts, b->insts.data(), b->insts.size() * sizeof(BInst), cudaMemcpyHostToDevice), "upload");
   if (!rc) rc = check_cuda(cudaMemcpy(b->d_stages, b->stages.data(), b->stages.size() * sizeof(BStage), cudaMemcpyHostToDevice), "upload");
+  if (!rc && !b->groups.empty()) rc = check_cuda(cudaMemcpy(b->d_groups, b->groups.data(), b->groups.size() * sizeof(BGroup), cudaMemcpyHostToDevice), "upload");
   if (!rc) rc = check_cuda(cudaMemcpy(b->d_order, b->order.data(), b->count * sizeof(int), cudaMemcpyHostToDevice), "upload");
   if (rc) return rc;
   // grid: CTAs per SM from the tune; every CTA owns a global slot
@@ -553,7 +633,8 @@ static int batch_enqueue(qcs_cuda_batch *b) {
   const size_t smem = smem_for(b->tune.tile_q);
   const int tq = b->tune.tile_q;
 #define QCS_LAUNCH_BATCH(T)                                                                       \
-  k_batch<T><<<b->grid, T, smem, b->stream>>>(b->d_insts, b->d_stages, b->d_gates, b->d_order,     \
+  k_batch<T><<<b->grid, T, smem, b->stream>>>(b->d_insts, b->d_stages, b->d_groups, b->d_gates,    \
+                                              b->d_order,                                          \
                                               b->count, b->shots, b->seed, tq, b->d_slots,         \
                                               (i64)b->slot_amps, b->d_queue, b->d_z,               \
                                               b->d_samples)
