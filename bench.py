@@ -336,6 +336,7 @@ def run_ours(args, dist):
         state.sample(draws)
     state.synchronize()
     dist.barrier()
+    x0 = state.transfer_bytes()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         state.set_basis(0)
@@ -343,6 +344,9 @@ def run_ours(args, dist):
         samples = state.sample(draws)
         top = state.argmax()
     e2e_s = dist.max(time.perf_counter() - t0)
+    x1 = state.transfer_bytes()
+    h2d_step = (x1[0] - x0[0]) // args.steps
+    d2h_step = (x1[1] - x0[1]) // args.steps
     del samples, top
 
     world = dist.world
@@ -422,8 +426,11 @@ def run_ours(args, dist):
         "parity": parity,
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT,
-                "h2d_bytes_per_step": int(draws.nbytes),
-                "d2h_bytes_per_step": int(shots * 8 + 8 + 16),
+                "h2d_bytes_per_step": int(h2d_step),
+                "d2h_bytes_per_step": int(d2h_step),
+                "bytes_source": "the library's own transfer counters (qcs_cuda_transfer_bytes): "
+                                "block-matrix images, 2x2 gate matrices, shot draws up; "
+                                "samples and results down",
                 "path": "qcs_cuda_set_basis + qcs_cuda_run(host op list) + "
                         "qcs_cuda_sample(1024 host draws) + qcs_cuda_argmax, host wall clock"},
         "gpu_launches": launches,

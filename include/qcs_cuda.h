@@ -127,6 +127,12 @@ int qcs_cuda_state_info(const qcs_cuda_state *s, int *num_qubits,
                         int *precision, int *semantics);
 /* The state's cudaStream_t, as void*. */
 int qcs_cuda_state_stream(qcs_cuda_state *s, void **stream);
+/* Bytes moved between host and device for this state since it was created:
+ * explicit copies (amplitude reads and writes, results, shot draws and
+ * samples, tensor-core block images) and the gate and block matrices carried
+ * in kernel parameters.  No reference counterpart (the reference's state is
+ * host memory). */
+int qcs_cuda_transfer_bytes(qcs_cuda_state *s, long long *h2d, long long *d2h);
 /* Device address of the live amplitude buffer (valid until the next call
  * that may swap buffers in REFERENCE semantics). */
 int qcs_cuda_state_device_ptr(qcs_cuda_state *s, void **ptr);

@@ -89,6 +89,7 @@ def _declare(L):
         "qcs_cuda_phase_flip": (i, [vp, ll]),
         "qcs_cuda_diffusion": (i, [vp]),
         "qcs_cuda_run": (i, [vp, vp, i, C.POINTER(RunOptions)]),
+        "qcs_cuda_transfer_bytes": (i, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "qcs_cuda_norm_sq": (i, [vp, dp]),
         "qcs_cuda_normalize": (i, [vp]),
         "qcs_cuda_prob_zero": (i, [vp, i, dp]),
@@ -252,6 +253,12 @@ class State:
         opt = RunOptions(fusion_k, engine, partitioner, 0 if plan_cache else RUN_NO_PLAN_CACHE)
         _check(lib().qcs_cuda_run(self._h, ops.ctypes.data_as(C.c_void_p), len(ops),
                                   C.byref(opt)))
+
+    def transfer_bytes(self):
+        """(host->device, device->host) bytes moved for this state so far."""
+        a, b = C.c_longlong(), C.c_longlong()
+        _check(lib().qcs_cuda_transfer_bytes(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def norm_sq(self) -> float:
         x = C.c_double()

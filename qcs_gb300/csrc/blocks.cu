@@ -174,6 +174,7 @@ static int launch_block(qcs_cuda_state *s, const TileGeom &g, const double *u) {
   i64 want = g.n_tiles;
   i64 cap = (i64)s->dev.num_sms * 8;
   int grid = (int)(want < cap ? want : cap);
+  s->h2d_bytes += (long long)sizeof(U);  // the block matrix rides in the parameters
   prof_begin(s);
   k_block_simt<C, K><<<grid, kBlockThreads, smem, s->stream>>>((C *)s->vec, g, U);
   return launched(s, KC_BLOCK_SIMT, 2.0 * s->size * sizeof(C), "apply_block (SIMT)");

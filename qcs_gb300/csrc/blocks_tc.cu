@@ -779,8 +779,7 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
   if (k == 6) make_image<64>(u, h);
   else make_image<32>(u, h);
   const size_t used = k == 6 ? TcShape<64>::IMG_BYTES : TcShape<32>::IMG_BYTES;
-  rc = check_cuda(cudaMemcpyAsync(d, h, used, cudaMemcpyHostToDevice, s->stream),
-                  "block image upload");
+  rc = copy_h2d(s, d, h, used, "block image upload");
   if (rc) return rc;
   const uint4 *img = reinterpret_cast<const uint4 *>(d);
   const int renorm = (known_unitary || unitarity_defect(u, KA) < 1e-9) ? 1 : 0;

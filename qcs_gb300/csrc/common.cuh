@@ -88,6 +88,10 @@ struct qcs_cuda_state {
   int *d_err;             // device error flag (bounded waits that gave up)
   qcs_cuda_costmodel *cm; // model for QCS_PARTITION_LEARNED (not owned)
   qcs::PlanCache *plans;  // last fused run's plan and block matrices
+  // bytes moved between host and device on this state's behalf: explicit
+  // copies and the matrices carried in kernel parameters
+  long long h2d_bytes;
+  long long d2h_bytes;
 };
 
 namespace qcs {
@@ -95,6 +99,9 @@ namespace qcs {
 // ---- status / errors ------------------------------------------------------
 int set_error(int status, const char *fmt, ...);
 int check_cuda(cudaError_t e, const char *what);
+// Host <-> device copies on the state's stream, counted in h2d/d2h_bytes.
+int copy_h2d(qcs_cuda_state *s, void *dst, const void *src, size_t bytes, const char *what);
+int copy_d2h(qcs_cuda_state *s, void *dst, const void *src, size_t bytes, const char *what);
 int check_launch(const char *what);
 // Every kernel launch on a state is bracketed by these two calls:
 // prof_begin before the launch, launched() after it (checks the launch,

@@ -245,13 +245,20 @@ static int apply_ctrl_t(qcs_cuda_state *s, const double m[8], int c, int t) {
   return launched(s, KC_CTRL1Q, Ns, "apply_controlled");
 }
 
+// The 2x2 travels in the kernel's parameters: 4 complex values.
+static void count_matrix(qcs_cuda_state *s) {
+  s->h2d_bytes += s->prec == QCS_CUDA_C128 ? 64 : 32;
+}
+
 int apply_1q(qcs_cuda_state *s, const double m[8], int t) {
   invalidate_sum(s);
+  count_matrix(s);
   return s->prec == QCS_CUDA_C128 ? apply_1q_t<double2>(s, m, t) : apply_1q_t<float2>(s, m, t);
 }
 
 int apply_ctrl(qcs_cuda_state *s, const double m[8], int c, int t) {
   invalidate_sum(s);
+  count_matrix(s);
   return s->prec == QCS_CUDA_C128 ? apply_ctrl_t<double2>(s, m, c, t)
                                   : apply_ctrl_t<float2>(s, m, c, t);
 }

@@ -432,9 +432,7 @@ static int reduce(qcs_cuda_state *s, int op, int q, double *res, int nres) {
   k_finalize<<<1, 32, 0, s->stream>>>(s->d_partials, d.reduce_blocks, dst);
   rc = launched(s, KC_OTHER, d.reduce_blocks * 32.0, "reduce finalize");
   if (rc || !res) return rc;
-  rc = check_cuda(cudaMemcpyAsync(s->h_result, s->d_result, 8 * sizeof(double),
-                                  cudaMemcpyDeviceToHost, s->stream),
-                  "reduce readback");
+  rc = copy_d2h(s, s->h_result, s->d_result, 8 * sizeof(double), "reduce readback");
   if (!rc) rc = check_cuda(cudaStreamSynchronize(s->stream), "reduce sync");
   if (rc) return rc;
   for (int i = 0; i < nres; i++) res[i] = s->h_result[(op == OP_SUM ? 4 : 0) + i];
@@ -581,9 +579,8 @@ int qcs_cuda_probability(qcs_cuda_state *s, long long index, double *p) {
     return QCS_CUDA_OK;
   }
   size_t bytes = s->prec == QCS_CUDA_C128 ? 16 : 8;
-  int rc = check_cuda(cudaMemcpyAsync(s->h_result, (char *)s->vec + (size_t)index * bytes, bytes,
-                                      cudaMemcpyDeviceToHost, s->stream),
-                      "probability readback");
+  int rc = copy_d2h(s, s->h_result, (char *)s->vec + (size_t)index * bytes, bytes,
+                    "probability readback");
   if (!rc) rc = check_cuda(cudaStreamSynchronize(s->stream), "probability sync");
   if (rc) return rc;
   if (s->prec == QCS_CUDA_C128) {
@@ -613,9 +610,7 @@ int qcs_cuda_argmax(qcs_cuda_state *s, long long *index, double *prob) {
   prof_begin(s);
   k_argmax_finalize<<<1, 32, 0, s->stream>>>(s->d_partials, d.reduce_blocks, s->d_result);
   rc = launched(s, KC_OTHER, d.reduce_blocks * 32.0, "argmax finalize");
-  if (!rc) rc = check_cuda(cudaMemcpyAsync(s->h_result, s->d_result, 2 * sizeof(double),
-                                           cudaMemcpyDeviceToHost, s->stream),
-                           "argmax readback");
+  if (!rc) rc = copy_d2h(s, s->h_result, s->d_result, 2 * sizeof(double), "argmax readback");
   if (!rc) rc = check_cuda(cudaStreamSynchronize(s->stream), "argmax sync");
   if (rc) return rc;
   *index = (long long)s->h_result[1];
@@ -649,9 +644,7 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
   rc = launched(s, KC_SAMPLE, 16.0 * s->n_tiles, "sample prefix");
   if (rc) return rc;
   memcpy(s->h_draws, random_vals, (size_t)shots * sizeof(double));
-  rc = check_cuda(cudaMemcpyAsync(s->d_draws, s->h_draws, (size_t)shots * sizeof(double),
-                                  cudaMemcpyHostToDevice, s->stream),
-                  "sample draws upload");
+  rc = copy_h2d(s, s->d_draws, s->h_draws, (size_t)shots * sizeof(double), "sample draws upload");
   if (rc) return rc;
   int threads = 256;
   int blocks = (int)(((i64)shots * 32 + threads - 1) / threads);
@@ -666,9 +659,8 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
                                                        s->d_tile_prefix, s->d_draws, shots,
                                                        s->d_samples);
   rc = launched(s, KC_SAMPLE, (double)shots * tile * sb, "sample");
-  if (!rc) rc = check_cuda(cudaMemcpyAsync(s->h_samples, s->d_samples, (size_t)shots * sizeof(i64),
-                                           cudaMemcpyDeviceToHost, s->stream),
-                           "sample readback");
+  if (!rc) rc = copy_d2h(s, s->h_samples, s->d_samples, (size_t)shots * sizeof(i64),
+                         "sample readback");
   if (!rc) rc = check_cuda(cudaStreamSynchronize(s->stream), "sample sync");
   if (rc) return rc;
   memcpy(out_index, s->h_samples, (size_t)shots * sizeof(i64));

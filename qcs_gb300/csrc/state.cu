@@ -167,6 +167,16 @@ void prof_begin(qcs_cuda_state *s) {
   cudaEventRecord(p->open, s->stream);
 }
 
+int copy_h2d(qcs_cuda_state *s, void *dst, const void *src, size_t bytes, const char *what) {
+  s->h2d_bytes += (long long)bytes;
+  return check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->stream), what);
+}
+
+int copy_d2h(qcs_cuda_state *s, void *dst, const void *src, size_t bytes, const char *what) {
+  s->d2h_bytes += (long long)bytes;
+  return check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s->stream), what);
+}
+
 int launched(qcs_cuda_state *s, int cls, double bytes, const char *what) {
   int rc = check_launch(what);
   s->launches++;
@@ -358,6 +368,13 @@ int qcs_cuda_state_stream(qcs_cuda_state *s, void **stream) {
   return QCS_CUDA_OK;
 }
 
+int qcs_cuda_transfer_bytes(qcs_cuda_state *s, long long *h2d, long long *d2h) {
+  QCS_CHECK_STATE(s);
+  if (h2d) *h2d = s->h2d_bytes;
+  if (d2h) *d2h = s->d2h_bytes;
+  return QCS_CUDA_OK;
+}
+
 int qcs_cuda_state_device_ptr(qcs_cuda_state *s, void **ptr) {
   QCS_CHECK_STATE(s);
   if (!ptr) return set_error(QCS_CUDA_EINVAL, "null out");
@@ -370,6 +387,7 @@ int qcs_cuda_synchronize(qcs_cuda_state *s) {
   int rc = check_cuda(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
   if (rc) return rc;
   int flag = 0;
+  s->d2h_bytes += (long long)sizeof(int);
   rc = check_cuda(cudaMemcpy(&flag, s->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
   if (rc) return rc;
   if (flag) {
@@ -405,17 +423,14 @@ int qcs_cuda_read_amplitudes(qcs_cuda_state *s, long long first, long long count
   int rc = check_cuda(cudaStreamSynchronize(s->stream), "sync before read");
   if (rc) return rc;
   if (s->prec == QCS_CUDA_C128) {
-    rc = check_cuda(cudaMemcpyAsync(out, (double2 *)s->vec + first, (size_t)count * 16,
-                                    cudaMemcpyDeviceToHost, s->stream),
-                    "cudaMemcpy(read)");
+    rc = copy_d2h(s, out, (double2 *)s->vec + first, (size_t)count * 16, "cudaMemcpy(read)");
     return rc ? rc : check_cuda(cudaStreamSynchronize(s->stream), "sync after read");
   }
   std::vector<float2> tmp((size_t)(count < kCopyChunk ? count : kCopyChunk));
   for (i64 off = 0; off < count; off += kCopyChunk) {
     i64 m = count - off < kCopyChunk ? count - off : kCopyChunk;
-    rc = check_cuda(cudaMemcpyAsync(tmp.data(), (float2 *)s->vec + first + off, (size_t)m * 8,
-                                    cudaMemcpyDeviceToHost, s->stream),
-                    "cudaMemcpy(read)");
+    rc = copy_d2h(s, tmp.data(), (float2 *)s->vec + first + off, (size_t)m * 8,
+                  "cudaMemcpy(read)");
     if (!rc) rc = check_cuda(cudaStreamSynchronize(s->stream), "sync after read");
     if (rc) return rc;
     for (i64 i = 0; i < m; i++) {
@@ -437,9 +452,7 @@ int qcs_cuda_write_amplitudes(qcs_cuda_state *s, long long first, long long coun
   if (rc) return rc;
   invalidate_sum(s);
   if (s->prec == QCS_CUDA_C128) {
-    rc = check_cuda(cudaMemcpyAsync((double2 *)s->vec + first, in, (size_t)count * 16,
-                                    cudaMemcpyHostToDevice, s->stream),
-                    "cudaMemcpy(write)");
+    rc = copy_h2d(s, (double2 *)s->vec + first, in, (size_t)count * 16, "cudaMemcpy(write)");
     return rc ? rc : check_cuda(cudaStreamSynchronize(s->stream), "sync after write");
   }
   std::vector<float2> tmp((size_t)(count < kCopyChunk ? count : kCopyChunk));
@@ -447,9 +460,8 @@ int qcs_cuda_write_amplitudes(qcs_cuda_state *s, long long first, long long coun
     i64 m = count - off < kCopyChunk ? count - off : kCopyChunk;
     for (i64 i = 0; i < m; i++)
       tmp[i] = make_float2((float)in[2 * (off + i)], (float)in[2 * (off + i) + 1]);
-    rc = check_cuda(cudaMemcpyAsync((float2 *)s->vec + first + off, tmp.data(), (size_t)m * 8,
-                                    cudaMemcpyHostToDevice, s->stream),
-                    "cudaMemcpy(write)");
+    rc = copy_h2d(s, (float2 *)s->vec + first + off, tmp.data(), (size_t)m * 8,
+                  "cudaMemcpy(write)");
     if (!rc) rc = check_cuda(cudaStreamSynchronize(s->stream), "sync after write");
     if (rc) return rc;
   }
