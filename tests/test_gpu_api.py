@@ -292,3 +292,30 @@ def test_64bit_extensions(A):
     assert A.qc_sample_shots(c, 4, samples) == 0
     assert list(samples) == [(1 << 31) - 5] * 4
     A.qc_destroy(c)
+
+
+def test_transfer_counters():
+    """qcs_cuda_transfer_bytes counts what crosses the host/device boundary:
+    amplitude writes and reads, shot draws and samples, the 2x2 matrices in
+    kernel parameters and the tensor-core block images."""
+    from qcs_gb300 import capi
+    n = 14
+    with capi.State(n, capi.C64) as s:
+        h0, d0 = s.transfer_bytes()
+        s.set_amplitudes(np.ones(1 << n) / np.sqrt(1 << n))
+        h1, d1 = s.transfer_bytes()
+        assert h1 - h0 == 8 << n and d1 == d0
+        s.amplitudes()
+        h2, d2 = s.transfer_bytes()
+        assert d2 - d1 == 8 << n and h2 == h1
+        s.apply_gate(capi.W.H, 3)
+        h3, _ = s.transfer_bytes()
+        assert h3 - h2 == 32
+        u, _ = np.linalg.qr(np.random.default_rng(1).normal(size=(64, 64)) + 0j)
+        s.apply_block(list(range(6)), u, capi.FUSE_TENSOR)
+        h4, _ = s.transfer_bytes()
+        assert h4 - h3 == 2 * 128 * 128 * 2  # bf16 hi + lo image of the 128 x 128 real form
+        draws = np.linspace(0.01, 0.99, 100)
+        s.sample(draws)
+        h5, d5 = s.transfer_bytes()
+        assert h5 - h4 == 800 and d5 - d2 == 800
