@@ -65,6 +65,8 @@ def parse():
                          "QFT + 64 Grover iterations at --qubits (33/34); batch: 4096 "
                          "variational instances in one persistent launch")
     ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batch: keep the default schedule (512 threads, tile 2^13, 2 CTAs/SM)")
     ap.add_argument("--shots", type=int, default=1024)
     return ap.parse_args()
 
@@ -675,7 +677,7 @@ def run_batch(args, dist):
     inst = W.variational_batch(args.instances, args.seed)
     mine = inst[dist.rank::dist.world]
     with capi.Batch(mine, shots=args.shots, seed=args.seed) as b:
-        tune = b.autotune(repeats=1)
+        tune = b.autotune(repeats=1) if not args.no_autotune else "default"
         for _ in range(args.warmup):
             b.run()
         dist.barrier()

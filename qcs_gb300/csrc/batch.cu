@@ -98,7 +98,11 @@ struct qcs_cuda_batch {
   std::vector<qcs::BInst> insts;
   std::vector<qcs::BStage> stages;
   std::vector<qcs::BGroup> groups;
-  std::vector<int> gate_op;       // op index of every planned gate (group order)
+  // planned gates in group order: gate i is the product of the ops
+  // fold_ops[fold_off[i] .. fold_off[i+1]) (one-qubit gates on one qubit with
+  // nothing else on that qubit between them fold into one 2x2)
+  std::vector<int> fold_off;
+  std::vector<int> fold_ops;
   std::vector<int> gate_tc;       // its group-local target | control << 8 (control 0xFF: none)
   std::vector<int> order;
   qcs::BatchTune tune;
@@ -452,7 +456,7 @@ static void plan_groups(qcs_cuda_batch *b, const std::vector<int> &stage_ops, in
   for (const PlanItem &it : items) {
     BGroup G;
     memset(&G, 0, sizeof(G));
-    G.gate0 = (int)b->gate_op.size();
+    G.gate0 = (int)b->gate_tc.size();
     G.r = (int)it.qubits.size();
     for (int j = 0; j < G.r; j++) G.q[j] = (signed char)tile_bit(it.qubits[j]);
     auto group_bit = [&](int q) {
@@ -460,14 +464,35 @@ static void plan_groups(qcs_cuda_batch *b, const std::vector<int> &stage_ops, in
         if (it.qubits[j] == q) return j;
       return -1;
     };
+    // gates of the group in order; pending[j]: index (in this group's gate
+    // list) of the one-qubit gate on group bit j that later one-qubit gates
+    // on j fold into, -1 after a two-qubit gate touched j
+    std::vector<std::vector<int>> glist;
+    std::vector<int> gtc;
+    int pending[kGroupQ];
+    for (int j = 0; j < kGroupQ; j++) pending[j] = -1;
     for (int g : it.gates) {
       const qcs_cuda_op &o = sub[g];
       const int t = group_bit(o.target);
-      const int c = gate_is_controlled(o.kind) ? group_bit(o.control) : 0xFF;
-      b->gate_op.push_back(stage_ops[g]);
-      b->gate_tc.push_back(t | (c << 8));
+      if (gate_is_controlled(o.kind)) {
+        const int c = group_bit(o.control);
+        pending[t] = pending[c] = -1;
+        glist.push_back({stage_ops[g]});
+        gtc.push_back(t | (c << 8));
+      } else if (pending[t] >= 0) {
+        glist[pending[t]].push_back(stage_ops[g]);
+      } else {
+        pending[t] = (int)glist.size();
+        glist.push_back({stage_ops[g]});
+        gtc.push_back(t | (0xFF << 8));
+      }
     }
-    G.ngates = (int)b->gate_op.size() - G.gate0;
+    for (size_t e = 0; e < glist.size(); e++) {
+      b->fold_off.push_back((int)b->fold_ops.size());
+      for (int op : glist[e]) b->fold_ops.push_back(op);
+      b->gate_tc.push_back(gtc[e]);
+    }
+    G.ngates = (int)b->gate_tc.size() - G.gate0;
     b->groups.push_back(G);
   }
   st.ngroups = (int)b->groups.size() - st.group0;
@@ -477,7 +502,8 @@ static int batch_plan(qcs_cuda_batch *b, int tile_q) {
   b->insts.clear();
   b->stages.clear();
   b->groups.clear();
-  b->gate_op.clear();
+  b->fold_off.clear();
+  b->fold_ops.clear();
   b->gate_tc.clear();
   for (int i = 0; i < b->count; i++) {
     BInst I;
@@ -534,20 +560,40 @@ static int batch_plan(qcs_cuda_batch *b, int tile_q) {
     }
     b->insts.push_back(I);
   }
+  b->fold_off.push_back((int)b->fold_ops.size());
   b->planned_tile_q = tile_q;
   return QCS_CUDA_OK;
 }
 
-// Gate table from the ops and the current angles (group-local bits).
+// Gate table from the ops and the current angles (group-local bits): each
+// entry is the FP64 product of its folded ops, rounded once to FP32.
 static void batch_fill_gates(qcs_cuda_batch *b) {
-  for (size_t gi = 0; gi < b->gate_op.size(); gi++) {
-    const qcs_cuda_op &o = b->ops[b->gate_op[gi]];
-    double m[8];
-    gate_matrix(o.kind, o.angle, m);
+  const size_t ng = b->gate_tc.size();
+  for (size_t gi = 0; gi < ng; gi++) {
+    double acc[8] = {1, 0, 0, 0, 0, 0, 1, 0};
+    int kind = 0;
+    for (int f = b->fold_off[gi]; f < b->fold_off[gi + 1]; f++) {
+      const qcs_cuda_op &o = b->ops[b->fold_ops[f]];
+      kind = o.kind;
+      double m[8], r[8];
+      gate_matrix(o.kind, o.angle, m);
+      for (int i = 0; i < 2; i++)  // acc := m * acc
+        for (int j = 0; j < 2; j++) {
+          double re = 0.0, im = 0.0;
+          for (int l = 0; l < 2; l++) {
+            const double *x = m + 2 * (2 * i + l), *y = acc + 2 * (2 * l + j);
+            re += x[0] * y[0] - x[1] * y[1];
+            im += x[0] * y[1] + x[1] * y[0];
+          }
+          r[2 * (2 * i + j)] = re;
+          r[2 * (2 * i + j) + 1] = im;
+        }
+      memcpy(acc, r, sizeof(acc));
+    }
     BGate g;
     memset(&g, 0, sizeof(g));
-    for (int e = 0; e < 4; e++) g.m[e] = make_float2((float)m[2 * e], (float)m[2 * e + 1]);
-    g.type = gate_is_controlled(o.kind) ? 1 : 0;
+    for (int e = 0; e < 4; e++) g.m[e] = make_float2((float)acc[2 * e], (float)acc[2 * e + 1]);
+    g.type = gate_is_controlled(kind) ? 1 : 0;
     g.t = b->gate_tc[gi] & 0xFF;
     g.c = g.type ? (b->gate_tc[gi] >> 8) & 0xFF : 0;
     b->h_gates[gi] = g;
@@ -585,8 +631,8 @@ static int batch_upload(qcs_cuda_batch *b) {
   int rc = check_cuda(cudaMalloc((void **)&b->d_insts, b->insts.size() * sizeof(BInst)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_stages, b->stages.size() * sizeof(BStage)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_groups, std::max<size_t>(1, b->groups.size()) * sizeof(BGroup)), "cudaMalloc(batch)");
-  if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_gates, std::max<size_t>(1, b->gate_op.size()) * sizeof(BGate)), "cudaMalloc(batch)");
-  if (!rc) rc = check_cuda(cudaMallocHost((void **)&b->h_gates, std::max<size_t>(1, b->gate_op.size()) * sizeof(BGate)), "cudaMallocHost(batch)");
+  if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_gates, std::max<size_t>(1, b->gate_tc.size()) * sizeof(BGate)), "cudaMalloc(batch)");
+  if (!rc) rc = check_cuda(cudaMallocHost((void **)&b->h_gates, std::max<size_t>(1, b->gate_tc.size()) * sizeof(BGate)), "cudaMallocHost(batch)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_order, b->count * sizeof(int)), "cudaMalloc(batch)");
   if (rc) return rc;
   batch_fill_gates(b);
@@ -625,7 +671,7 @@ static int batch_upload(qcs_cuda_batch *b) {
 }
 
 static int batch_enqueue(qcs_cuda_batch *b) {
-  const size_t gbytes = std::max<size_t>(1, b->gate_op.size()) * sizeof(BGate);
+  const size_t gbytes = std::max<size_t>(1, b->gate_tc.size()) * sizeof(BGate);
   int rc = check_cuda(cudaMemcpyAsync(b->d_gates, b->h_gates, gbytes, cudaMemcpyHostToDevice, b->stream),
                       "batch gate upload");
   if (!rc) rc = check_cuda(cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream), "batch queue reset");
