@@ -677,7 +677,7 @@ def run_batch(args, dist):
     inst = W.variational_batch(args.instances, args.seed)
     mine = inst[dist.rank::dist.world]
     with capi.Batch(mine, shots=args.shots, seed=args.seed) as b:
-        tune = b.autotune(repeats=1) if not args.no_autotune else "default"
+        tune = b.autotune(repeats=1) if not args.no_autotune else b.schedule()
         for _ in range(args.warmup):
             b.run()
         dist.barrier()

@@ -237,10 +237,19 @@ int qcs_cuda_batch_set_angles(qcs_cuda_batch *b, const double *angles);
 int qcs_cuda_batch_run(qcs_cuda_batch *b, double *expect_z0,
                        long long *samples, double *ms);
 /* Times every schedule (threads per CTA 256/512/1024, tile 2^12..2^14,
- * 1 or 2 CTAs per SM, largest-first or given order) on this batch and keeps
- * the fastest; chosen (4 ints) receives it. */
+ * 1 or 2 CTAs per SM, largest-first or given order) on this batch, then how
+ * widely large instances spread (an instance above split_q qubits is shared
+ * by 2^(n - split_q) CTAs, split_q in 17..20 or never), and keeps the
+ * fastest; chosen (4 ints) receives threads, tile qubits, CTAs per SM and
+ * order. */
 int qcs_cuda_batch_autotune(qcs_cuda_batch *b, int repeats, int *chosen);
-/* Sets one schedule explicitly. */
+/* The schedule in force (5 ints): threads, tile qubits, CTAs per SM that
+ * actually run, order, split_q. */
+int qcs_cuda_batch_schedule(qcs_cuda_batch *b, int *schedule);
+/* Instances above split_q qubits (and above the tile) are shared by
+ * 2^(n - split_q) CTAs, at most half the grid; 27 never splits. */
+int qcs_cuda_batch_split(qcs_cuda_batch *b, int split_q);
+/* Sets one schedule explicitly (split_q is kept). */
 int qcs_cuda_batch_config(qcs_cuda_batch *b, int threads, int tile_q,
                           int ctas_per_sm, int order);
 

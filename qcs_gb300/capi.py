@@ -112,6 +112,8 @@ def _declare(L):
         "qcs_cuda_batch_run": (i, [vp, dp, llp, dp]),
         "qcs_cuda_batch_autotune": (i, [vp, i, ip]),
         "qcs_cuda_batch_config": (i, [vp, i, i, i, i]),
+        "qcs_cuda_batch_schedule": (i, [vp, ip]),
+        "qcs_cuda_batch_split": (i, [vp, i]),
         "qcs_cuda_costmodel_create": (i, [i, C.c_ulonglong, vpp]),
         "qcs_cuda_costmodel_destroy": (i, [vp]),
         "qcs_cuda_costmodel_num_params": (i, [vp, ip]),
@@ -409,11 +411,20 @@ class Batch:
     def autotune(self, repeats: int = 2):
         out = (C.c_int * 4)()
         _check(lib().qcs_cuda_batch_autotune(self._h, repeats, out))
+        return self.schedule()
+
+    def schedule(self):
+        out = (C.c_int * 5)()
+        _check(lib().qcs_cuda_batch_schedule(self._h, out))
         return {"threads": out[0], "tile_q": out[1], "ctas_per_sm": out[2],
-                "order": "largest-first" if out[3] == 0 else "given"}
+                "order": "largest-first" if out[3] == 0 else "given",
+                "split_q": out[4]}
 
     def config(self, threads: int, tile_q: int, ctas_per_sm: int, order: int = 0):
         _check(lib().qcs_cuda_batch_config(self._h, threads, tile_q, ctas_per_sm, order))
+
+    def split(self, split_q: int):
+        _check(lib().qcs_cuda_batch_split(self._h, split_q))
 
 
 COSTMODEL_FEATURES = 20

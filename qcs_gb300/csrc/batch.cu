@@ -48,8 +48,11 @@ struct BInst {
   int n;
   int stage0;
   int nstages;
-  int shots_off;  // unused (shots are instance * shots)
+  int group;  // CTAs that share the instance's stages (1: one CTA)
 };
+
+// Bounded spin of one thread on a counter another CTA raises: ~2 s.
+constexpr long long kBatchWaitCycles = 4000000000LL;
 
 struct BStage {
   int group0;
@@ -82,6 +85,7 @@ struct BatchTune {
   int tile_q;       // 12, 13 or 14
   int ctas_per_sm;  // 1 or 2
   int order;        // 0: largest first, 1: given order
+  int split_q;      // instances above split_q qubits run on 2^(n - split_q) CTAs
 };
 
 }  // namespace qcs
@@ -104,7 +108,8 @@ struct qcs_cuda_batch {
   std::vector<int> fold_off;
   std::vector<int> fold_ops;
   std::vector<int> gate_tc;       // its group-local target | control << 8 (control 0xFF: none)
-  std::vector<int> order;
+  std::vector<int> order;         // instance order
+  std::vector<int2> items;        // (instance, member) in queue order
   qcs::BatchTune tune;
   int planned_tile_q;
   // device
@@ -115,8 +120,10 @@ struct qcs_cuda_batch {
   qcs::BGroup *d_groups;
   qcs::BGate *d_gates;
   qcs::BGate *h_gates;  // pinned; the graph's upload node reads it
-  int *d_order;
+  int2 *d_items;
   int *d_queue;
+  int *d_stage_done;  // per instance: member stage completions this launch
+  int *d_lead;        // per instance: 1 + CTA of member 0 (its slot holds the state)
   double *d_z;
   double *h_z;          // pinned
   qcs::i64 *d_samples;
@@ -172,6 +179,12 @@ __device__ double block_sum(double v, double *red) {
   return r;  // valid in thread 0
 }
 
+// Shared-memory position of tile amplitude i: the low 4 bits are XORed with
+// the next 4, a bijection that spreads a warp's accesses over the banks
+// whichever tile bits a gate group holds (without it, a group on bits 0..3
+// sends all 32 lanes of a warp to one bank).
+__device__ __forceinline__ int swz(int i) { return i ^ ((i >> 4) & 15); }
+
 // One 2x2 on register bit TB of the R amplitudes a[] (controlled: only where
 // register bit c is set).  Static indices keep a[] in registers.
 template <int R, int TB>
@@ -210,7 +223,7 @@ __device__ __forceinline__ void smem_group_r(float2 *S, int nt, const BGroup &G,
     };
     float2 a[1 << kGroupQ];
 #pragma unroll
-    for (int e = 0; e < R; e++) a[e] = S[off(e)];
+    for (int e = 0; e < R; e++) a[e] = S[swz(off(e))];
     for (int gi = 0; gi < G.ngates; gi++) {
       const BGate g = gates[G.gate0 + gi];
       switch (g.t) {
@@ -221,7 +234,7 @@ __device__ __forceinline__ void smem_group_r(float2 *S, int nt, const BGroup &G,
       }
     }
 #pragma unroll
-    for (int e = 0; e < R; e++) S[off(e)] = a[e];
+    for (int e = 0; e < R; e++) S[swz(off(e))] = a[e];
   }
 }
 
@@ -293,36 +306,72 @@ __device__ void smem_prefix(double *x, int m) {
   __syncthreads();
 }
 
+// Thread 0 waits until *cnt >= target (bounded); false on timeout or abort.
+__device__ bool wait_count(const int *cnt, int target, int *err, int where) {
+  const long long t0 = clock64();
+  while (*(volatile const int *)cnt < target) {
+    if (*(volatile const int *)err) return false;
+    if (clock64() - t0 > kBatchWaitCycles) {
+      atomicCAS(err, 0, where);
+      return false;
+    }
+    __nanosleep(200);
+  }
+  __threadfence();
+  return true;
+}
+
 // 64 registers a thread: two CTAs of 512 threads (or one of 1024) fit an SM.
+// Work items are (instance, member): an instance of `group` > 1 is shared by
+// `group` CTAs that split the tiles of each stage and meet at a counter
+// after every stage; the grid never exceeds the CTAs that fit the GPU at
+// once, so every member of a group runs concurrently with the others.
 template <int T>
 __global__ void __launch_bounds__(T, 1024 / T)
     k_batch(const BInst *insts, const BStage *stages, const BGroup *groups, const BGate *gates,
-            const int *order,
-            int count, int shots, u64 seed, int tile_q, float2 *slots, i64 slot_amps,
-            int *queue, double *z_out, i64 *samples_out) {
+            const int2 *items, int n_items, int shots, u64 seed, int tile_q, float2 *slots,
+            i64 slot_amps, int *queue, int *stage_done, int *lead, int *err, double *z_out,
+            i64 *samples_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *S = reinterpret_cast<float2 *>(smem_raw);               // 2^tile_q amplitudes
   double *prefix = reinterpret_cast<double *>(S + (1 << tile_q));  // up to 1025 tile masses
   __shared__ double red[T / 32];
-  __shared__ int s_inst;
+  __shared__ int s_item;
+  __shared__ int s_ok;
   __shared__ i64 goff_lo[64];
   __shared__ i64 goff_hi[256];
-  float2 *slot = slots + (i64)blockIdx.x * slot_amps;
 
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) s_inst = atomicAdd(queue, 1);
+    if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
     __syncthreads();
-    const int qi = s_inst;
-    if (qi >= count) break;
-    const int inst = order[qi];
+    const int qi = s_item;
+    if (qi >= n_items) break;
+    const int inst = items[qi].x;
+    const int member = items[qi].y;
     const BInst I = insts[inst];
+    const int G = I.group;
     const i64 size = 1LL << I.n;
     double z = 0.0;
+    // the instance's amplitudes live in the slot of its member-0 CTA
+    float2 *slot = slots + (i64)blockIdx.x * slot_amps;
+    if (G > 1) {
+      if (threadIdx.x == 0) {
+        s_ok = 1;
+        if (member == 0) {
+          atomicExch(&lead[inst], blockIdx.x + 1);
+        } else {
+          s_ok = wait_count(&lead[inst], 1, err, 1) ? 1 : 0;
+        }
+      }
+      __syncthreads();
+      if (!s_ok) return;
+      slot = slots + (i64)(*(volatile int *)&lead[inst] - 1) * slot_amps;
+    }
     if (I.n <= tile_q) {
       // ---- shared-memory resident instance ----
       const int L = 1 << I.n;
-      for (int i = threadIdx.x; i < L; i += T) S[i] = make_float2(i == 0 ? 1.f : 0.f, 0.f);
+      for (int i = threadIdx.x; i < L; i += T) S[swz(i)] = make_float2(i == 0 ? 1.f : 0.f, 0.f);
       __syncthreads();
       const BStage st = stages[I.stage0];
       for (int gi = 0; gi < st.ngroups; gi++) {
@@ -335,7 +384,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
         double zp = 0.0, mp = 0.0;
         for (int j = threadIdx.x; j < tile; j += T) {
           const int i = t * tile + j;
-          const float2 a = S[i];
+          const float2 a = S[swz(i)];
           const float p = a.x * a.x + a.y * a.y;
           mp += (double)p;
           zp += (i & 1) ? -(double)p : (double)p;
@@ -349,7 +398,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
       }
       smem_prefix<T>(prefix, n_tiles);
       sample_shots<T>(prefix, n_tiles, tile, shots, seed, inst, samples_out + (i64)inst * shots,
-                      [&](i64 i) { return S[i]; });
+                      [&](i64 i) { return S[swz((int)i)]; });
     } else {
       // ---- global-slot instance, run in stages ----
       for (int si = 0; si < I.nstages; si++) {
@@ -385,22 +434,35 @@ __global__ void __launch_bounds__(T, 1024 / T)
           }
         }
         const i64 n_tiles = 1LL << nout;
-        for (i64 tt = 0; tt < n_tiles; tt++) {
+        for (i64 tt = member; tt < n_tiles; tt += G) {
           i64 base = 0;
           for (int j = 0; j < nout; j++) base |= ((tt >> j) & 1LL) << outside[j];
           for (int l = threadIdx.x; l < L; l += T) {
             const i64 gidx = base + goff_lo[l & 63] + goff_hi[l >> 6];
-            S[l] = si == 0 ? make_float2(gidx == 0 ? 1.f : 0.f, 0.f) : slot[gidx];
+            S[swz(l)] = si == 0 ? make_float2(gidx == 0 ? 1.f : 0.f, 0.f) : slot[gidx];
           }
           __syncthreads();
           for (int gi = 0; gi < st.ngroups; gi++) {
             smem_group<T>(S, nt, groups[st.group0 + gi], gates);
             __syncthreads();
           }
-          for (int l = threadIdx.x; l < L; l += T) slot[base + goff_lo[l & 63] + goff_hi[l >> 6]] = S[l];
+          for (int l = threadIdx.x; l < L; l += T)
+            slot[base + goff_lo[l & 63] + goff_hi[l >> 6]] = S[swz(l)];
           __syncthreads();
         }
+        if (G > 1) {  // every member's tiles of this stage are written
+          __threadfence();  // each thread's slot writes, before the count
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(&stage_done[inst], 1);
+            s_ok = wait_count(&stage_done[inst], G * (si + 1), err, 2) ? 1 : 0;
+          }
+          __syncthreads();
+          if (!s_ok) return;
+        }
       }
+      if (member != 0) continue;  // member 0 reads out the instance
       __threadfence_block();
       __syncthreads();
       // <Z_0> and tile masses in one contiguous pass (deterministic order);
@@ -509,7 +571,7 @@ static int batch_plan(qcs_cuda_batch *b, int tile_q) {
     BInst I;
     I.n = b->nq[i];
     I.stage0 = (int)b->stages.size();
-    I.shots_off = 0;
+    I.group = 1;
     const qcs_cuda_op *ops = b->ops.data() + b->op_off[i];
     const int nops = b->op_off[i + 1] - b->op_off[i];
     if (I.n <= tile_q) {
@@ -608,13 +670,13 @@ static void batch_free_device(qcs_cuda_batch *b) {
   cudaFree(b->d_groups);
   cudaFree(b->d_gates);
   if (b->h_gates) cudaFreeHost(b->h_gates);
-  cudaFree(b->d_order);
+  cudaFree(b->d_items);
   b->d_insts = nullptr;
   b->d_stages = nullptr;
   b->d_groups = nullptr;
   b->d_gates = nullptr;
   b->h_gates = nullptr;
-  b->d_order = nullptr;
+  b->d_items = nullptr;
 }
 
 static size_t smem_for(int tile_q) { return ((size_t)8 << tile_q) + 1025 * sizeof(double); }
@@ -633,9 +695,37 @@ static int batch_upload(qcs_cuda_batch *b) {
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_groups, std::max<size_t>(1, b->groups.size()) * sizeof(BGroup)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_gates, std::max<size_t>(1, b->gate_tc.size()) * sizeof(BGate)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMallocHost((void **)&b->h_gates, std::max<size_t>(1, b->gate_tc.size()) * sizeof(BGate)), "cudaMallocHost(batch)");
-  if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_order, b->count * sizeof(int)), "cudaMalloc(batch)");
   if (rc) return rc;
   batch_fill_gates(b);
+  // grid: CTAs per SM from the tune, but never more than fit the GPU at once
+  // (members of a group wait for each other); every CTA owns a global slot
+  int fit = 0;
+  switch (b->tune.threads) {
+    case 256: rc = set_smem_attr<256>(b->tune.tile_q); break;
+    case 512: rc = set_smem_attr<512>(b->tune.tile_q); break;
+    default: rc = set_smem_attr<1024>(b->tune.tile_q); break;
+  }
+  if (rc) return rc;
+  switch (b->tune.threads) {
+    case 256: rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batch<256>, 256, smem_for(b->tune.tile_q)), "occupancy"); break;
+    case 512: rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batch<512>, 512, smem_for(b->tune.tile_q)), "occupancy"); break;
+    default: rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batch<1024>, 1024, smem_for(b->tune.tile_q)), "occupancy"); break;
+  }
+  if (rc) return rc;
+  if (fit < 1) return set_error(QCS_CUDA_EUNSUP, "batch kernel does not fit an SM");
+  const int grid = b->dev.num_sms * std::min(b->tune.ctas_per_sm, fit);
+  // group sizes: 2^(n - split_q) CTAs above split_q qubits (never below the
+  // tile, at most half the grid)
+  for (int i = 0; i < b->count; i++) {
+    BInst &I = b->insts[i];
+    int G = 1;
+    if (I.n > b->tune.tile_q && I.n > b->tune.split_q) {
+      const int e = I.n - b->tune.split_q;
+      G = e >= 20 ? (1 << 20) : (1 << e);
+      G = std::min(G, std::max(1, grid / 2));
+    }
+    I.group = G;
+  }
   // instance order
   b->order.resize(b->count);
   std::iota(b->order.begin(), b->order.end(), 0);
@@ -649,10 +739,12 @@ static int batch_upload(qcs_cuda_batch *b) {
   rc = check_cuda(cudaMemcpy(b->d_insts, b->insts.data(), b->insts.size() * sizeof(BInst), cudaMemcpyHostToDevice), "upload");
   if (!rc) rc = check_cuda(cudaMemcpy(b->d_stages, b->stages.data(), b->stages.size() * sizeof(BStage), cudaMemcpyHostToDevice), "upload");
   if (!rc && !b->groups.empty()) rc = check_cuda(cudaMemcpy(b->d_groups, b->groups.data(), b->groups.size() * sizeof(BGroup), cudaMemcpyHostToDevice), "upload");
-  if (!rc) rc = check_cuda(cudaMemcpy(b->d_order, b->order.data(), b->count * sizeof(int), cudaMemcpyHostToDevice), "upload");
+  b->items.clear();
+  for (int inst : b->order)
+    for (int g = 0; g < b->insts[inst].group; g++) b->items.push_back(make_int2(inst, g));
+  if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_items, b->items.size() * sizeof(int2)), "cudaMalloc(batch)");
+  if (!rc) rc = check_cuda(cudaMemcpy(b->d_items, b->items.data(), b->items.size() * sizeof(int2), cudaMemcpyHostToDevice), "upload");
   if (rc) return rc;
-  // grid: CTAs per SM from the tune; every CTA owns a global slot
-  const int grid = b->dev.num_sms * b->tune.ctas_per_sm;
   if (grid != b->grid) {
     cudaFree(b->d_slots);
     b->d_slots = nullptr;
@@ -662,11 +754,6 @@ static int batch_upload(qcs_cuda_batch *b) {
     rc = check_cuda(cudaMalloc((void **)&b->d_slots, slot * grid * sizeof(float2)), "cudaMalloc(batch slots)");
     if (rc) return rc;
   }
-  switch (b->tune.threads) {
-    case 256: rc = set_smem_attr<256>(b->tune.tile_q); break;
-    case 512: rc = set_smem_attr<512>(b->tune.tile_q); break;
-    default: rc = set_smem_attr<1024>(b->tune.tile_q); break;
-  }
   return rc;
 }
 
@@ -675,15 +762,17 @@ static int batch_enqueue(qcs_cuda_batch *b) {
   int rc = check_cuda(cudaMemcpyAsync(b->d_gates, b->h_gates, gbytes, cudaMemcpyHostToDevice, b->stream),
                       "batch gate upload");
   if (!rc) rc = check_cuda(cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream), "batch queue reset");
+  if (!rc) rc = check_cuda(cudaMemsetAsync(b->d_stage_done, 0, b->count * sizeof(int), b->stream), "batch counters");
+  if (!rc) rc = check_cuda(cudaMemsetAsync(b->d_lead, 0, b->count * sizeof(int), b->stream), "batch counters");
+  if (!rc) rc = check_cuda(cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream), "batch error flag");
   if (rc) return rc;
   const size_t smem = smem_for(b->tune.tile_q);
   const int tq = b->tune.tile_q;
 #define QCS_LAUNCH_BATCH(T)                                                                       \
-  k_batch<T><<<b->grid, T, smem, b->stream>>>(b->d_insts, b->d_stages, b->d_groups, b->d_gates,    \
-                                              b->d_order,                                          \
-                                              b->count, b->shots, b->seed, tq, b->d_slots,         \
-                                              (i64)b->slot_amps, b->d_queue, b->d_z,               \
-                                              b->d_samples)
+  k_batch<T><<<b->grid, T, smem, b->stream>>>(                                                    \
+      b->d_insts, b->d_stages, b->d_groups, b->d_gates, b->d_items, (int)b->items.size(),           \
+      b->shots, b->seed, tq, b->d_slots, (i64)b->slot_amps, b->d_queue, b->d_stage_done, b->d_lead, \
+      b->d_err, b->d_z, b->d_samples)
   switch (b->tune.threads) {
     case 256: QCS_LAUNCH_BATCH(256); break;
     case 512: QCS_LAUNCH_BATCH(512); break;
@@ -742,11 +831,25 @@ static int batch_launch_timed(qcs_cuda_batch *b, float *ms) {
   return rc;
 }
 
+// A timed replay whose device error flag is checked afterwards.
+static int batch_launch_checked(qcs_cuda_batch *b, float *ms) {
+  int rc = batch_launch_timed(b, ms);
+  if (rc) return rc;
+  int flag = 0;
+  rc = check_cuda(cudaMemcpy(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost), "batch error flag");
+  if (rc) return rc;
+  if (flag)
+    return set_error(QCS_CUDA_ETIMEOUT, "batch: a group of CTAs gave up waiting (site %d)", flag);
+  return QCS_CUDA_OK;
+}
+
 static void batch_destroy(qcs_cuda_batch *b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
   batch_free_device(b);
   cudaFree(b->d_queue);
+  cudaFree(b->d_stage_done);
+  cudaFree(b->d_lead);
   cudaFree(b->d_z);
   cudaFree(b->d_samples);
   cudaFree(b->d_slots);
@@ -805,6 +908,9 @@ int qcs_cuda_batch_create(int count, const int *num_qubits, const int *op_offset
   if (!rc) rc = device_info(dev, &b->dev);
   if (!rc) rc = check_cuda(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_queue, sizeof(int)), "cudaMalloc(batch)");
+  if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_stage_done, count * sizeof(int)), "cudaMalloc(batch)");
+  if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_lead, count * sizeof(int)), "cudaMalloc(batch)");
+  if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_err, sizeof(int)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&b->d_z, count * sizeof(double)), "cudaMalloc(batch)");
   if (!rc) rc = check_cuda(cudaMallocHost((void **)&b->h_z, count * sizeof(double)), "cudaMallocHost(batch)");
   if (!rc && shots > 0) {
@@ -816,6 +922,7 @@ int qcs_cuda_batch_create(int count, const int *num_qubits, const int *op_offset
   t.tile_q = 13;
   t.ctas_per_sm = 2;
   t.order = 0;
+  t.split_q = 19;
   if (!rc) rc = batch_apply_tune(b, t);
   if (rc) {
     batch_destroy(b);
@@ -843,7 +950,7 @@ int qcs_cuda_batch_set_angles(qcs_cuda_batch *b, const double *angles) {
 int qcs_cuda_batch_run(qcs_cuda_batch *b, double *expect_z0, long long *samples, double *ms) {
   if (!b) return set_error(QCS_CUDA_EINVAL, "null batch");
   float t = 0.f;
-  int rc = batch_launch_timed(b, &t);
+  int rc = batch_launch_checked(b, &t);
   if (rc) return rc;
   b->last_ms = t;
   if (ms) *ms = t;
@@ -856,6 +963,17 @@ int qcs_cuda_batch_run(qcs_cuda_batch *b, double *expect_z0, long long *samples,
 int qcs_cuda_batch_autotune(qcs_cuda_batch *b, int repeats, int *chosen) {
   if (!b) return set_error(QCS_CUDA_EINVAL, "null batch");
   if (repeats < 1) repeats = 1;
+  auto time_tune = [&](const BatchTune &t, float *out) {
+    int rc = batch_apply_tune(b, t);
+    float ms = 0.f, sum = 0.f;
+    if (!rc) rc = batch_launch_checked(b, &ms);  // warm-up
+    for (int r = 0; !rc && r < repeats; r++) {
+      rc = batch_launch_checked(b, &ms);
+      sum += ms;
+    }
+    *out = sum / repeats;
+    return rc;
+  };
   const int threads[] = {256, 512, 1024};
   const int tiles[] = {12, 13, 14};
   const int ctas[] = {1, 2};
@@ -867,26 +985,34 @@ int qcs_cuda_batch_autotune(qcs_cuda_batch *b, int repeats, int *chosen) {
         for (int ord = 0; ord < 2; ord++) {
           // two CTAs per SM must fit in shared memory
           if (cp == 2 && smem_for(tq) * 2 > 220 * 1024) continue;
-          BatchTune t;
+          BatchTune t = b->tune;
           t.threads = th;
           t.tile_q = tq;
           t.ctas_per_sm = cp;
           t.order = ord;
-          int rc = batch_apply_tune(b, t);
+          float ms = 0.f;
+          int rc = time_tune(t, &ms);
           if (rc) return rc;
-          float sum = 0.f, ms = 0.f;
-          rc = batch_launch_timed(b, &ms);  // warm-up
-          if (rc) return rc;
-          for (int r = 0; r < repeats; r++) {
-            rc = batch_launch_timed(b, &ms);
-            if (rc) return rc;
-            sum += ms;
-          }
-          if (sum / repeats < best_ms) {
-            best_ms = sum / repeats;
+          if (ms < best_ms) {
+            best_ms = ms;
             best = t;
           }
         }
+  // then how far large instances spread over CTAs (27: never)
+  const int splits[] = {17, 18, 19, 20, 27};
+  const BatchTune base = best;
+  for (int sq : splits) {
+    if (sq == base.split_q) continue;
+    BatchTune t = base;
+    t.split_q = sq;
+    float ms = 0.f;
+    int rc = time_tune(t, &ms);
+    if (rc) return rc;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = t;
+    }
+  }
   int rc = batch_apply_tune(b, best);
   if (rc) return rc;
   if (chosen) {
@@ -898,6 +1024,24 @@ int qcs_cuda_batch_autotune(qcs_cuda_batch *b, int repeats, int *chosen) {
   return QCS_CUDA_OK;
 }
 
+int qcs_cuda_batch_split(qcs_cuda_batch *b, int split_q) {
+  if (!b) return set_error(QCS_CUDA_EINVAL, "null batch");
+  if (split_q < 1 || split_q > 27) return set_error(QCS_CUDA_EINVAL, "split_q %d outside 1..27", split_q);
+  BatchTune t = b->tune;
+  t.split_q = split_q;
+  return batch_apply_tune(b, t);
+}
+
+int qcs_cuda_batch_schedule(qcs_cuda_batch *b, int *schedule) {
+  if (!b || !schedule) return set_error(QCS_CUDA_EINVAL, "null argument");
+  schedule[0] = b->tune.threads;
+  schedule[1] = b->tune.tile_q;
+  schedule[2] = std::min(b->tune.ctas_per_sm, b->grid / std::max(1, b->dev.num_sms));
+  schedule[3] = b->tune.order;
+  schedule[4] = b->tune.split_q;
+  return QCS_CUDA_OK;
+}
+
 int qcs_cuda_batch_config(qcs_cuda_batch *b, int threads, int tile_q, int ctas_per_sm,
                           int order) {
   if (!b) return set_error(QCS_CUDA_EINVAL, "null batch");
@@ -906,7 +1050,7 @@ int qcs_cuda_batch_config(qcs_cuda_batch *b, int threads, int tile_q, int ctas_p
     return set_error(QCS_CUDA_EINVAL, "bad batch schedule");
   if (ctas_per_sm == 2 && smem_for(tile_q) * 2 > 220 * 1024)
     return set_error(QCS_CUDA_EINVAL, "two CTAs of tile 2^%d do not fit one SM", tile_q);
-  BatchTune t;
+  BatchTune t = b->tune;
   t.threads = threads;
   t.tile_q = tile_q;
   t.ctas_per_sm = ctas_per_sm;

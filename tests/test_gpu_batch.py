@@ -66,6 +66,28 @@ def test_batch_matches_oracle(schedule):
     assert sum(p <= 0.01 for p in pvals) <= 2, sorted(pvals)[:5]
 
 
+@pytest.mark.parametrize("split_q", [12, 13])
+def test_batch_instances_shared_by_groups_of_ctas(split_q):
+    """Instances above the tile run on groups of 2^(n - split_q) CTAs that
+    split every stage's tiles and meet at a counter between stages; the
+    results equal the oracle's and, bit for bit, the one-CTA results."""
+    inst = W.variational_batch(24, seed=12, n_range=(13, 16), depth_range=(3, 6))
+    with capi.Batch(inst, shots=1024, seed=4) as b:
+        b.config(512, 12, 2, 0)
+        b.split(27)
+        z1, s1, _ = b.run()
+        b.split(split_q)
+        sched = b.schedule()
+        z2, s2, _ = b.run()
+        z3, s3, _ = b.run()
+    assert sched["split_q"] == split_q
+    assert np.array_equal(z2, z3) and np.array_equal(s2, s3)
+    assert np.array_equal(z1, z2) and np.array_equal(s1, s2)
+    for i, (n, g) in enumerate(inst[:8]):
+        zo, _ = oracle_instance(n, g)
+        assert abs(z2[i] - zo) < 1e-5
+
+
 def test_batch_set_angles_and_autotune():
     inst = W.variational_batch(24, seed=8, n_range=(8, 16), depth_range=(2, 5))
     with capi.Batch(inst, shots=256, seed=3) as b:
