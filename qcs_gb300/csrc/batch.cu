@@ -77,7 +77,7 @@ struct BGate {
   float2 m[4];
   int type;  // 0: 2x2 on group bit t; 1: 2x2 on group bit t where bit c is set
   int t, c;
-  int pad;
+  int form;  // 0: dense; 1: exchange (X, CNOT: m = [[0,1],[1,0]]); 2: diagonal
 };
 
 struct BatchTune {
@@ -189,13 +189,32 @@ __device__ __forceinline__ int swz(int i) { return i ^ ((i >> 4) & 15); }
 // register bit c is set).  Static indices keep a[] in registers.
 template <int R, int TB>
 __device__ __forceinline__ void reg_gate(float2 (&a)[1 << kGroupQ], const BGate &g) {
+  if (g.form == 1) {  // exchange: no arithmetic
 #pragma unroll
-  for (int e = 0; e < R; e++) {
-    if (e & (1 << TB)) continue;
-    if (g.type && !((e >> g.c) & 1)) continue;
-    const float2 v0 = a[e], v1 = a[e | (1 << TB)];
-    a[e] = cadd(cmul(g.m[0], v0), cmul(g.m[1], v1));
-    a[e | (1 << TB)] = cadd(cmul(g.m[2], v0), cmul(g.m[3], v1));
+    for (int e = 0; e < R; e++) {
+      if (e & (1 << TB)) continue;
+      if (g.type && !((e >> g.c) & 1)) continue;
+      const float2 v0 = a[e];
+      a[e] = a[e | (1 << TB)];
+      a[e | (1 << TB)] = v0;
+    }
+  } else if (g.form == 2) {  // diagonal: one complex product per amplitude
+#pragma unroll
+    for (int e = 0; e < R; e++) {
+      if (e & (1 << TB)) continue;
+      if (g.type && !((e >> g.c) & 1)) continue;
+      a[e] = cmul(g.m[0], a[e]);
+      a[e | (1 << TB)] = cmul(g.m[3], a[e | (1 << TB)]);
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < R; e++) {
+      if (e & (1 << TB)) continue;
+      if (g.type && !((e >> g.c) & 1)) continue;
+      const float2 v0 = a[e], v1 = a[e | (1 << TB)];
+      a[e] = cadd(cmul(g.m[0], v0), cmul(g.m[1], v1));
+      a[e | (1 << TB)] = cadd(cmul(g.m[2], v0), cmul(g.m[3], v1));
+    }
   }
 }
 
@@ -656,6 +675,12 @@ static void batch_fill_gates(qcs_cuda_batch *b) {
     memset(&g, 0, sizeof(g));
     for (int e = 0; e < 4; e++) g.m[e] = make_float2((float)acc[2 * e], (float)acc[2 * e + 1]);
     g.type = gate_is_controlled(kind) ? 1 : 0;
+    // exact zeros decide the form: the exchange and diagonal paths give the
+    // same numbers as the dense one (the skipped terms are products with 0)
+    const bool off0 = acc[2] == 0.0 && acc[3] == 0.0 && acc[4] == 0.0 && acc[5] == 0.0;
+    const bool swap = acc[0] == 0.0 && acc[1] == 0.0 && acc[6] == 0.0 && acc[7] == 0.0 &&
+                      acc[2] == 1.0 && acc[3] == 0.0 && acc[4] == 1.0 && acc[5] == 0.0;
+    g.form = swap ? 1 : (off0 ? 2 : 0);
     g.t = b->gate_tc[gi] & 0xFF;
     g.c = g.type ? (b->gate_tc[gi] >> 8) & 0xFF : 0;
     b->h_gates[gi] = g;
