@@ -305,9 +305,10 @@ int qcs_cuda_collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops,
 int qcs_cuda_state_set_costmodel(qcs_cuda_state *s, qcs_cuda_costmodel *m);
 /* Host only: the learned plan for a num_qubits state (order/item as in
  * qcs_cuda_plan), the model's predicted ms for it and for the greedy
- * width-kmax plan, and which candidate won (2..7: greedy width; 100 + k:
- * model-stopped growth at width k), plus 1000 x the number of that
- * candidate's blocks the model then split into narrower items. */
+ * width-kmax plan, and which candidate won: the greedy width k (2..7), plus
+ * 100 when the model stopped blocks from growing, plus 200 when ties were
+ * broken by lookahead, plus 1000 x the number of that candidate's blocks the
+ * model then split into narrower items. */
 int qcs_cuda_plan_learned(const qcs_cuda_op *ops, int count, int num_qubits,
                           int kmax, qcs_cuda_costmodel *m, int *order,
                           int *item, int *num_items, double *pred_ms,

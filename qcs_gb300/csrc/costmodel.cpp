@@ -161,23 +161,24 @@ std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n
   std::vector<PlanItem> best = partition(ops, count, n, po);
   const double judge = plan_ms(ps, best);
   double best_ms = judge;
-  int best_choice = kmax;  // 2..7: greedy width; 100 + k: model-stopped growth
-  for (int k = 2; k <= kmax; k++) {
-    // greedy at a smaller width, and model-stopped growth at each width
-    for (int grown = 0; grown < 2; grown++) {
-      if (!grown && k == kmax) continue;
-      po.kmax = k;
-      po.cost = grown ? grow_cost : nullptr;
-      po.cost_ctx = grown ? &ps : nullptr;
-      std::vector<PlanItem> cand = partition(ops, count, n, po);
-      const double t = plan_ms(ps, cand);
-      if (t < best_ms) {
-        best_ms = t;
-        best = std::move(cand);
-        best_choice = grown ? 100 + k : k;
+  // 2..7: greedy width; + 100: model-stopped growth; + 200: lookahead ties
+  int best_choice = kmax;
+  for (int k = 2; k <= kmax; k++)
+    for (int tie = 0; tie < 2; tie++)
+      for (int grown = 0; grown < 2; grown++) {
+        if (!grown && !tie && k == kmax) continue;  // the judge itself
+        po.kmax = k;
+        po.tie = tie;
+        po.cost = grown ? grow_cost : nullptr;
+        po.cost_ctx = grown ? &ps : nullptr;
+        std::vector<PlanItem> cand = partition(ops, count, n, po);
+        const double t = plan_ms(ps, cand);
+        if (t < best_ms) {
+          best_ms = t;
+          best = std::move(cand);
+          best_choice = k + (grown ? 100 : 0) + (tie ? 200 : 0);
+        }
       }
-    }
-  }
   // Block by block: split the blocks the model predicts slower than their
   // parts (a wide block holding a few diagonal gates, say).
   std::vector<PlanItem> refined;

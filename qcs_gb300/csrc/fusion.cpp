@@ -10,7 +10,8 @@
 //      on disjoint qubits.
 //   3. When no ready gate fits, close the block and go to 1.
 // With a cost hook, step 2 also stops when adding the gate would raise the
-// estimated time per gate of the block.
+// estimated time per gate of the block.  With tie = 1, step 2 breaks ties
+// between gates of equal growth by a one-step lookahead instead of by age.
 #include <algorithm>
 #include <cmath>
 
@@ -78,6 +79,27 @@ static void partition_segment(const qcs_cuda_op *ops, int first, int last, int n
       for (int q = 0; q < n; q++) if (inb[q]) qs.push_back(q);
       best_rate = opt.cost(n, kb, 1, qs.data(), opt.cost_ctx);
     }
+    // gates that fit the block at no growth once gate `cand` has joined it
+    auto lookahead = [&](int cand) {
+      std::vector<char> in2 = inb;
+      int qc[2];
+      const int mc = op_qubits(ops[cand], qc);
+      for (int j = 0; j < mc; j++) in2[qc[j]] = 1;
+      int score = 0;
+      for (int q2 = 0; q2 < n; q2++) {
+        if (!in2[q2]) continue;
+        size_t h = head[q2] + (next_on(q2) == cand ? 1 : 0);
+        for (; h < onq[q2].size(); h++) {
+          int qg[2];
+          const int mg = op_qubits(ops[onq[q2][h]], qg);
+          bool inside = true;
+          for (int j = 0; j < mg; j++) inside = inside && in2[qg[j]];
+          if (!inside) break;
+          score++;
+        }
+      }
+      return score;
+    };
     for (;;) {
       int best = -1, best_grow = 1 << 30;
       for (int q = 0; q < n; q++) {
@@ -88,9 +110,14 @@ static void partition_segment(const qcs_cuda_op *ops, int first, int last, int n
         int grow = 0;
         for (int j = 0; j < m; j++) grow += inb[qq[j]] ? 0 : 1;
         if (kb + grow > kmax) continue;
-        if (grow < best_grow || (grow == best_grow && g < best)) {
+        if (grow < best_grow) {
           best = g;
           best_grow = grow;
+        } else if (grow == best_grow && g != best) {
+          const bool take = (opt.tie == 1 && grow > 0) ? lookahead(g) > lookahead(best) ||
+                                                             (lookahead(g) == lookahead(best) && g < best)
+                                                       : g < best;
+          if (take) best = g;
         }
       }
       if (best < 0) break;

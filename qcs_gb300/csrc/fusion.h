@@ -34,6 +34,10 @@ struct PartitionOptions {
   int kmax;
   BlockCostFn cost;
   void *cost_ctx;
+  // Tie-break among ready gates that grow the block by the same (non-zero)
+  // number of qubits: 0 takes the earliest; 1 takes the one after which the
+  // most further gates fit the block at no growth (one step of lookahead).
+  int tie = 0;
 };
 
 // Greedy fixed-k partition of ops[0..count).
