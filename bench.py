@@ -570,11 +570,19 @@ def run_random20(args, dist):
             o.run(full)
             ref = o.amplitudes()
         cpu_s = time.perf_counter() - t0
+        # the reference's sequential mode: one core
+        prev = O.set_threads(1)
+        t0 = time.perf_counter()
+        with O.OracleState(n, omode) as o:
+            o.run(full)
+        cpu1_s = time.perf_counter() - t0
+        O.set_threads(prev)
         out[name] = {"gate_apps_per_s": len(full) / (ms / 1e3), "ms_per_circuit": ms,
                      "bit_exact": bool(np.array_equal(a.view(np.float64), ref.view(np.float64))),
                      "max_abs_err": float(np.max(np.abs(a - ref))),
                      "oracle_gate_apps_per_s": len(full) / cpu_s,
-                     "oracle_threads": os.cpu_count()}
+                     "oracle_threads": prev,
+                     "oracle_1thread_gate_apps_per_s": len(full) / cpu1_s}
     line = {"mode": "random20", "qubits": n, "dtype": "complex128", "gates": len(full),
             "seed": args.seed, "results": out,
             "note": "REFERENCE compares against the oracle's COMPAT mode, which is "

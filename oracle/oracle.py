@@ -42,6 +42,11 @@ def build(ref: bool = False) -> None:
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
 
+def set_threads(threads: int) -> int:
+    """OpenMP threads of the oracle's sweeps; returns the previous count."""
+    return lib().orc_set_threads(threads)
+
+
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
@@ -80,6 +85,7 @@ def lib() -> C.CDLL:
             "orc_grover_iterations": (i, [i]),
             "orc_qft": (None, [vp]),
             "orc_grover": (None, [vp, l, i]),
+            "orc_set_threads": (i, [i]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

@@ -10,6 +10,9 @@
 #include <string.h>
 
 #include "qcs_oracle.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 typedef struct {
   double re;
@@ -89,6 +92,21 @@ void orc_destroy(orc_state *s) {
 }
 
 int orc_num_qubits(const orc_state *s) { return s->n; }
+
+/* Threads of the OpenMP sweeps (timing of the CPU baseline: 1 = the
+ * reference's sequential mode, all cores = its OpenMP mode); returns the
+ * previous setting, 1 without OpenMP. */
+int orc_set_threads(int threads) {
+#ifdef _OPENMP
+  int prev = omp_get_max_threads();
+  if (threads > 0)
+    omp_set_num_threads(threads);
+  return prev;
+#else
+  (void)threads;
+  return 1;
+#endif
+}
 long orc_size(const orc_state *s) { return s->size; }
 int orc_mode(const orc_state *s) { return s->mode; }
 

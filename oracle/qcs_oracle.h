@@ -58,6 +58,7 @@ extern "C" {
 typedef struct orc_state orc_state;
 
 orc_state *orc_create(int num_qubits, int mode);
+int orc_set_threads(int threads);
 void orc_destroy(orc_state *s);
 int orc_num_qubits(const orc_state *s);
 long orc_size(const orc_state *s);
