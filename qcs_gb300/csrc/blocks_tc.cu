@@ -103,16 +103,29 @@ struct TcShape {
 struct TcGeom {
   i64 n_tiles;
   int nfree;
-  int nruns;          // contiguous runs of a tile (at most 64)
-  int run_bytes;      // bytes per run (>= 1 KB: the tile holds qubits 0..6)
+  int nruns;          // prefetch pieces of a tile (at most 128)
+  int run_bytes;      // bytes per piece (>= 512 B: the tile holds qubits 0..6)
+  int pf_ahead;       // tiles ahead whose pieces are prefetched
   signed char freeq[40];
   i64 col_off[kTcM];  // column m -> offset (bits of m on the column qubits)
   i64 blk_off[64];    // block index a -> offset (bit j of a on qubits[j])
-  i64 run_off[64];    // run j -> offset of its first amplitude
+  i64 run_off[128];   // piece j -> offset of its first amplitude
 };
 
-// Tiles ahead of the one being converted whose runs are prefetched into L2.
-constexpr int kPrefetchAhead = 2;
+// Prefetch shape (tuning knobs while measuring): tiles ahead, and the
+// largest prefetch piece as a power of two of amplitudes.
+static int env_int_or(const char *name, int dflt) {
+  const char *e = getenv(name);
+  return (e && *e) ? atoi(e) : dflt;
+}
+static int pf_ahead() {
+  static int v = env_int_or("QCS_TC_PF_AHEAD", 2);
+  return v;
+}
+static int pf_piece_bits() {
+  static int v = env_int_or("QCS_TC_PF_PIECE", 16);
+  return v;
+}
 
 __device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
   i64 b = 0;
@@ -275,8 +288,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // the runs of the tile kPrefetchAhead ahead go to L2 now, so that the
       // register loads issued for the next tile below find them there
       {
-        const i64 far = tile + (i64)kPrefetchAhead * gridDim.x;
-        if (p < g.nruns && far < g.n_tiles)
+        const i64 far = tile + (i64)g.pf_ahead * gridDim.x;
+        if (p < g.nruns && far < g.n_tiles)  // nruns <= 128 < 256 producers
           prefetch_l2(v + tile_base(far, g) + g.run_off[p], (uint32_t)g.run_bytes);
       }
       if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
@@ -593,14 +606,21 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
     int R = 0;
     while (R < (int)tq.size() && tq[R] == R) R++;
     const int nt = (int)tq.size();
-    g.nruns = 1 << (nt - R);
-    g.run_bytes = (int)(8LL << R);
+    // pieces: runs split down to at most 2^pf_piece amplitudes, at most 128
+    const int nrun_bits = nt - R;
+    int piece = R;
+    while (piece > pf_piece_bits() && nrun_bits + (R - piece) < 7) piece--;
+    g.nruns = 1 << (nrun_bits + (R - piece));
+    g.run_bytes = (int)(8LL << piece);
     for (int j = 0; j < g.nruns; j++) {
-      i64 o = 0;
+      const int sub = j & ((1 << (R - piece)) - 1);  // piece within its run
+      const int run = j >> (R - piece);
+      i64 o = (i64)sub << piece;
       for (int b = R; b < nt; b++)
-        if ((j >> (b - R)) & 1) o |= 1LL << tq[b];
+        if ((run >> (b - R)) & 1) o |= 1LL << tq[b];
       g.run_off[j] = o;
     }
+    g.pf_ahead = pf_ahead();
   }
   bool low = true;  // the block is exactly qubits 0..k-1
   for (int j = 0; j < k; j++) low = low && qubits[j] == j;
