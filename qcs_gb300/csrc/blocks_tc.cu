@@ -112,20 +112,12 @@ struct TcGeom {
   i64 run_off[128];   // piece j -> offset of its first amplitude
 };
 
-// Prefetch shape (tuning knobs while measuring): tiles ahead, and the
-// largest prefetch piece as a power of two of amplitudes.
-static int env_int_or(const char *name, int dflt) {
-  const char *e = getenv(name);
-  return (e && *e) ? atoi(e) : dflt;
-}
-static int pf_ahead() {
-  static int v = env_int_or("QCS_TC_PF_AHEAD", 2);
-  return v;
-}
-static int pf_piece_bits() {
-  static int v = env_int_or("QCS_TC_PF_PIECE", 16);
-  return v;
-}
+// Prefetch shape, measured at 30 qubits over six block placements (mean of
+// measured HBM fraction; two runs agreed within 1 %): 2 tiles ahead with
+// pieces of at most 2^9 amplitudes (4 KB) 0.922; whole runs 0.918; 2^8-
+// amplitude pieces 0.885; 3 tiles ahead 0.85-0.92 depending on the piece.
+static int pf_ahead() { return 2; }
+static int pf_piece_bits() { return 9; }
 
 __device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
   i64 b = 0;
