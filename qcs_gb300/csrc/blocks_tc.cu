@@ -27,8 +27,9 @@
 //               32w..32w+31 = tile columns), store FP32 results to HBM;
 //   warps 4-11  producers: load the tile's amplitudes from HBM, split into
 //               bf16 hi/lo, write the 128-byte-swizzled K-major operand tile;
-//               the block matrix stays resident in shared memory; a
-//               producer issues its HBM loads before waiting for a free stage
+//               the block matrix stays resident in shared memory; loads run
+//               one tile ahead in registers, and 2 tiles ahead the tile's
+//               contiguous pieces are bulk-prefetched into L2
 //   warp 12     TMEM allocation and MMA issue (one thread).
 // Operand tiles and TMEM accumulators are double buffered; stages hand over
 // through mbarriers.  Every wait is bounded: on expiry the kernel raises a
@@ -36,9 +37,9 @@
 // drained and TMEM is freed before exit.
 //
 // Shared memory (k = 6): 2 stages x (hi + lo) x 32 KB state tiles + 64 KB
-// block matrix (hi + lo) + tables ~= 197 KB.  HBM traffic: one read and one
-// write of the state per block, the same as the SIMT engine; tensor work per
-// amplitude 3 x 8 x 2^k flops.
+// block matrix (hi + lo) + tables, the column-norm ring and the low-mode
+// staging = 215 KB.  HBM traffic: one read and one write of the state per
+// block; tensor work per amplitude 3 x 8 x 2^k flops.
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdlib.h>
