@@ -113,12 +113,14 @@ struct TcGeom {
   i64 run_off[128];   // piece j -> offset of its first amplitude
 };
 
-// Prefetch shape, measured at 30 qubits over six block placements (mean of
-// measured HBM fraction; two runs agreed within 1 %): 2 tiles ahead with
-// pieces of at most 2^9 amplitudes (4 KB) 0.922; whole runs 0.918; 2^8-
-// amplitude pieces 0.885; 3 tiles ahead 0.85-0.92 depending on the piece.
+// Prefetch shape, measured at 30 qubits over six k = 6 block placements
+// (mean fraction of measured HBM; two runs agreed within 1 %): 2 tiles ahead
+// with whole runs 0.918, with pieces of at most 2^9 amplitudes 0.922, 2^8
+// 0.885, 3 tiles ahead 0.85-0.92 depending on the piece.  Whole runs are
+// kept: on the 30-qubit brick benchmark pieces of 2^9 measured 1.5 % slower,
+// and k = 5 blocks 14 % slower.
 static int pf_ahead() { return 2; }
-static int pf_piece_bits() { return 9; }
+static int pf_piece_bits() { return 16; }
 
 __device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
   i64 b = 0;
