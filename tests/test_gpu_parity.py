@@ -332,6 +332,32 @@ def test_apply_block_tensor_cores(k, placement):
             assert infidelity(a, b) < 1e-8
 
 
+@pytest.mark.parametrize("k,n", [(6, 13), (5, 12), (6, 14)])
+def test_tensor_cores_smallest_states(k, n):
+    """The smallest states the tensor engine takes (n = k + 7: one tile, one
+    CTA) and a few tiles: every pipeline stage runs with fewer tiles than
+    stages in flight."""
+    rng = np.random.default_rng(100 + n)
+    for placement in ("col", "pair", "low"):
+        if placement == "low":
+            qubits = list(range(k))
+        elif placement == "pair":
+            qubits = [0] + [int(q) for q in rng.choice(range(1, n), size=k - 1, replace=False)]
+        else:
+            qubits = [int(q) for q in rng.choice(range(1, n), size=k, replace=False)]
+        u, _ = np.linalg.qr(rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k)))
+        init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        init /= np.linalg.norm(init)
+        with capi.State(n, capi.C64) as s, O.OracleState(n) as o:
+            s.set_amplitudes(init)
+            o.set_amplitudes(init)
+            s.apply_block(qubits, u, capi.FUSE_TENSOR)
+            o.apply_block(qubits, u)
+            a, b = s.amplitudes(), o.amplitudes()
+            assert np.max(np.abs(a - b)) < TC_ATOL, placement
+            assert infidelity(a, b) < 1e-8, placement
+
+
 def test_auto_engine_widens_four_qubit_blocks():
     """AUTO runs a 4-qubit block on the tensor cores, widened to 5 qubits with
     the identity on the added qubit; fused circuits at width 4 likewise."""
