@@ -107,6 +107,7 @@ struct TcGeom {
   int nruns;          // prefetch pieces of a tile (at most 128)
   int run_bytes;      // bytes per piece (>= 512 B: the tile holds qubits 0..6)
   int pf_ahead;       // tiles ahead whose pieces are prefetched
+  int blocked;        // 1: each CTA walks a contiguous range of tiles; 0: cyclic
   signed char freeq[40];
   i64 col_off[kTcM];  // column m -> offset (bits of m on the column qubits)
   i64 blk_off[64];    // block index a -> offset (bit j of a on qubits[j])
@@ -120,12 +121,44 @@ struct TcGeom {
 // kept: on the 30-qubit brick benchmark pieces of 2^9 measured 1.5 % slower,
 // and k = 5 blocks 14 % slower.
 static int pf_ahead() { return 2; }
+// tile order knob while measuring (QCS_TC_ORDER=blocked)
+static int tile_order_blocked() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("QCS_TC_ORDER");
+    v = (e && strcmp(e, "blocked") == 0) ? 1 : 0;
+  }
+  return v;
+}
 static int pf_piece_bits() { return 16; }
 
 __device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
   i64 b = 0;
   for (int j = 0; j < g.nfree; j++) b |= ((tile >> j) & 1LL) << g.freeq[j];
   return b;
+}
+
+// The tiles one CTA processes, in order: tile(it) = start + it * stride for
+// it < count.  Cyclic: CTA b takes b, b + grid, ...; blocked: a contiguous
+// range, so that consecutive tiles of a CTA are adjacent in memory.
+struct TileWalk {
+  i64 start, stride, count;
+  __device__ __forceinline__ i64 at(i64 it) const { return start + it * stride; }
+};
+__device__ __forceinline__ TileWalk tile_walk(const TcGeom &g) {
+  const i64 b = blockIdx.x, G = gridDim.x;
+  TileWalk w;
+  if (g.blocked) {
+    const i64 per = g.n_tiles / G, rem = g.n_tiles % G;
+    w.start = b * per + (b < rem ? b : rem);
+    w.stride = 1;
+    w.count = per + (b < rem ? 1 : 0);
+  } else {
+    w.start = b;
+    w.stride = G;
+    w.count = b < g.n_tiles ? (g.n_tiles - b + G - 1) / G : 0;
+  }
+  return w;
 }
 
 // In kColMode and kPairMode a producer thread keeps one column (tile row
@@ -268,25 +301,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
       }
     };
-    int it = 0;
-    i64 tile = blockIdx.x;
-    if (tile < g.n_tiles) {
-      const i64 base = tile_base(tile, g);
+    const TileWalk w = tile_walk(g);
+    if (w.count > 0) {
+      const i64 base = tile_base(w.at(0), g);
       load_half(base, 0);
       load_half(base, 1);
     }
-    for (; tile < g.n_tiles; tile += gridDim.x, ++it) {
+    for (int it = 0; it < w.count; ++it) {
       const int stage = it & 1;
-      const i64 next = tile + gridDim.x;
-      const bool more = next < g.n_tiles;
-      const i64 nbase = more ? tile_base(next, g) : 0;
-      // the runs of the tile kPrefetchAhead ahead go to L2 now, so that the
-      // register loads issued for the next tile below find them there
-      {
-        const i64 far = tile + (i64)g.pf_ahead * gridDim.x;
-        if (p < g.nruns && far < g.n_tiles)  // nruns <= 128 < 256 producers
-          prefetch_l2(v + tile_base(far, g) + g.run_off[p], (uint32_t)g.run_bytes);
-      }
+      const bool more = it + 1 < w.count;
+      const i64 nbase = more ? tile_base(w.at(it + 1), g) : 0;
+      // the pieces of the tile pf_ahead ahead go to L2 now, so that the
+      // register loads issued for later tiles find them there
+      if (p < g.nruns && it + g.pf_ahead < w.count)  // nruns <= 128 < 256 producers
+        prefetch_l2(v + tile_base(w.at(it + g.pf_ahead), g) + g.run_off[p],
+                    (uint32_t)g.run_bytes);
       if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
       uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
       uint8_t *alo = ahi + S::A_BYTES;
@@ -337,8 +366,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(kTcM, S::N);
       const uint32_t a0 = smem_u32(sA), b_hi = smem_u32(sB), b_lo = b_hi + S::B_BYTES;
-      int it = 0;
-      for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
+      const TileWalk w = tile_walk(g);
+      for (int it = 0; it < w.count; ++it) {
         const int stage = it & 1;
         if (!wait_bar(bar(stage), (it >> 1) & 1, abort_flag, err, 2)) break;
         if (it >= 2 && !wait_bar(bar(4 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 3)) break;
@@ -371,8 +400,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // ---------------- epilogue ----------------
     const int m = tid;  // TMEM lane = tile column
     const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
-    int it = 0;
-    for (i64 tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++it) {
+    const TileWalk w = tile_walk(g);
+    for (int it = 0; it < w.count; ++it) {
+      const i64 tile = w.at(it);
       const int stage = it & 1;
       if (!wait_bar(bar(2 + stage), (it >> 1) & 1, abort_flag, err, 5)) break;
       // this tile's column norms; slot it % 4 cannot be refilled before this
@@ -616,6 +646,7 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
       g.run_off[j] = o;
     }
     g.pf_ahead = pf_ahead();
+    g.blocked = tile_order_blocked();
   }
   bool low = true;  // the block is exactly qubits 0..k-1
   for (int j = 0; j < k; j++) low = low && qubits[j] == j;
