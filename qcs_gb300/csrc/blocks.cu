@@ -30,7 +30,7 @@ int phase_flip(qcs_cuda_state *s, i64 index);
 int diffusion(qcs_cuda_state *s);
 int check_qubit(const qcs_cuda_state *s, int q, const char *what);
 int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u,
-                   bool known_unitary);
+                   bool known_unitary, const BlockFuse *fuse);
 bool tc_supported(const qcs_cuda_state *s, int k);
 
 constexpr int kBlockThreads = 128;  // = max columns per tile
@@ -223,22 +223,33 @@ static void widen_to_5(const qcs_cuda_state *s, int k, const int *qubits, const 
 // 3.0 ms for a 5-qubit tensor-core block.  `strict` (explicit
 // single-block calls) refuses a TENSOR request the tensor engine cannot
 // serve instead of running it on the CUDA cores.
+// The engine apply_block picks for a block of k qubits: 1 when the tensor
+// cores take it (widened to 5 qubits for k = 2..4), 0 for the CUDA cores.
+static bool block_on_tensor_cores(const qcs_cuda_state *s, int k, int engine) {
+  if (engine == QCS_FUSE_SIMT) return false;
+  if (tc_supported(s, k) && (engine == QCS_FUSE_TENSOR || k > 4)) return true;
+  return k >= 2 && k <= 4 && tc_supported(s, 5);
+}
+
 int apply_block(qcs_cuda_state *s, int k, const int *qubits, const double *u, int engine,
-                bool strict) {
-  invalidate_sum(s);
+                bool strict, const BlockFuse *fuse) {
   const bool tc_ok = tc_supported(s, k);
   const bool widen = engine != QCS_FUSE_SIMT && k >= 2 && k <= 4 && tc_supported(s, 5);
   if (engine == QCS_FUSE_TENSOR && strict && !tc_ok && !widen)
     return set_error(QCS_CUDA_EUNSUP, "tensor-core block engine: unsupported k=%d / precision", k);
-  // blocks from the planner (strict == false) are products of unitary gates
+  // blocks from the planner (strict == false) are products of unitary gates;
+  // the tensor-core path keeps or sets the cached sum itself
   if (tc_ok && (engine == QCS_FUSE_TENSOR || (engine == QCS_FUSE_AUTO && k > 4)))
-    return apply_block_tc(s, k, qubits, u, !strict);
+    return apply_block_tc(s, k, qubits, u, !strict, fuse);
   if (widen) {
     int q5[5];
     std::vector<double> u5;
     widen_to_5(s, k, qubits, u, q5, u5);
-    return apply_block_tc(s, 5, q5, u5.data(), !strict);
+    return apply_block_tc(s, 5, q5, u5.data(), !strict, fuse);
   }
+  if (fuse && (fuse->diffuse_in || fuse->sum_out))
+    return set_error(QCS_CUDA_EUNSUP, "fused diffusion needs the tensor-core engine");
+  invalidate_sum(s);
   if (s->prec == QCS_CUDA_C128) return apply_block_simt_t<double2>(s, k, qubits, u);
   return apply_block_simt_t<float2>(s, k, qubits, u);
 }
@@ -272,14 +283,14 @@ static int apply_op(qcs_cuda_state *s, const qcs_cuda_op &o) {
 }
 
 static int apply_block_item(qcs_cuda_state *s, const PlanItem &it, int engine,
-                            const std::vector<cd> &u);
+                            const std::vector<cd> &u, const BlockFuse *fuse);
 
 static int apply_item(qcs_cuda_state *s, const qcs_cuda_op *ops, const PlanItem &it, int engine,
                       std::vector<cd> &u) {
   if (it.kind == 1) return apply_op(s, ops[it.op]);
   if (it.gates.size() == 1) return apply_op(s, ops[it.gates[0]]);
   block_matrix(ops, it, u);
-  return apply_block_item(s, it, engine, u);
+  return apply_block_item(s, it, engine, u, nullptr);
 }
 
 static int fusion_cap(const qcs_cuda_state *s, int k, int engine) {
@@ -323,7 +334,7 @@ static bool plan_cache_hit(const PlanCache *c, const qcs_cuda_op *ops, int count
 static bool item_is_block(const PlanItem &it) { return it.kind == 0 && it.gates.size() > 1; }
 
 static int apply_block_item(qcs_cuda_state *s, const PlanItem &it, int engine,
-                            const std::vector<cd> &u) {
+                            const std::vector<cd> &u, const BlockFuse *fuse) {
   const int kb = (int)it.qubits.size();
   if (kb == 1) {
     double m[8] = {u[0].real(), u[0].imag(), u[1].real(), u[1].imag(),
@@ -331,7 +342,66 @@ static int apply_block_item(qcs_cuda_state *s, const PlanItem &it, int engine,
     return apply_1q(s, m, it.qubits[0]);
   }
   return apply_block(s, kb, it.qubits.data(), reinterpret_cast<const double *>(u.data()), engine,
-                     false);
+                     false, fuse);
+}
+
+static bool item_is_op(const qcs_cuda_op *ops, const PlanItem &it, int kind) {
+  return it.kind == 1 && ops[it.op].kind == kind;
+}
+
+// Executes a plan.  Two fusions across Grover-style barriers, for blocks the
+// tensor cores run: a diffusion directly followed by such a block runs
+// inside it (the block acts on 2m - psi), and such a block followed by phase
+// flips and then a diffusion leaves the amplitude sum that diffusion needs
+// (the flips correct it), so neither costs a pass over the state.  Block
+// matrices come from `use_mats` where present, else are formed here and,
+// within the budget, kept in `store_mats`.
+static int execute_plan(qcs_cuda_state *s, const qcs_cuda_op *ops,
+                        const std::vector<PlanItem> &plan, int engine,
+                        const std::vector<std::vector<cd>> *use_mats,
+                        std::vector<std::vector<cd>> *store_mats) {
+  auto on_tc = [&](const PlanItem &it) {
+    return item_is_block(it) && it.qubits.size() >= 2 &&
+           block_on_tensor_cores(s, (int)it.qubits.size(), engine);
+  };
+  std::vector<cd> u;
+  size_t kept = 0;
+  bool diffusion_pending = false;
+  for (size_t i = 0; i < plan.size(); i++) {
+    const PlanItem &it = plan[i];
+    int rc;
+    if (item_is_op(ops, it, QCS_OP_DIFFUSION) && i + 1 < plan.size() && on_tc(plan[i + 1])) {
+      diffusion_pending = true;  // applied by the next block
+      continue;
+    }
+    if (!item_is_block(it)) {
+      rc = apply_item(s, ops, it, engine, u);
+    } else {
+      BlockFuse f;
+      f.diffuse_in = diffusion_pending;
+      f.sum_out = false;
+      if (on_tc(it)) {
+        size_t j = i + 1;
+        while (j < plan.size() && item_is_op(ops, plan[j], QCS_OP_PHASE_FLIP)) j++;
+        f.sum_out = j < plan.size() && item_is_op(ops, plan[j], QCS_OP_DIFFUSION);
+      }
+      diffusion_pending = false;
+      const BlockFuse *fp = (f.diffuse_in || f.sum_out) ? &f : nullptr;
+      if (use_mats && !(*use_mats)[i].empty()) {
+        rc = apply_block_item(s, it, engine, (*use_mats)[i], fp);
+      } else {
+        block_matrix(ops, it, u);
+        rc = apply_block_item(s, it, engine, u, fp);
+        const size_t bytes = u.size() * sizeof(cd);
+        if (store_mats && kept + bytes <= kPlanCacheMatBytes) {
+          (*store_mats)[i] = u;
+          kept += bytes;
+        }
+      }
+    }
+    if (rc) return rc;
+  }
+  return QCS_CUDA_OK;
 }
 
 int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda_run_options *opt) {
@@ -352,17 +422,8 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
   const qcs_cuda_costmodel *cm = learned ? s->cm : nullptr;
   const unsigned long long gen = learned ? costmodel_generation(s->cm) : 0;
   const bool use_cache = !(opt->flags & QCS_RUN_NO_PLAN_CACHE);
-  if (use_cache && plan_cache_hit(s->plans, ops, count, s->n, k, engine, part, cm, gen)) {
-    const PlanCache &c = *s->plans;
-    std::vector<cd> u;
-    for (size_t i = 0; i < c.plan.size(); i++) {
-      const PlanItem &it = c.plan[i];
-      rc = (item_is_block(it) && !c.mats[i].empty()) ? apply_block_item(s, it, engine, c.mats[i])
-                                                     : apply_item(s, ops, it, engine, u);
-      if (rc) return rc;
-    }
-    return QCS_CUDA_OK;
-  }
+  if (use_cache && plan_cache_hit(s->plans, ops, count, s->n, k, engine, part, cm, gen))
+    return execute_plan(s, ops, s->plans->plan, engine, &s->plans->mats, nullptr);
   std::vector<PlanItem> plan;
   if (learned) {
     const bool simt_only = engine == QCS_FUSE_SIMT;
@@ -383,23 +444,8 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
     c->ops.assign(ops, ops + count);
     c->mats.assign(plan.size(), std::vector<cd>());
   }
-  size_t kept = 0;
-  std::vector<cd> u;
-  for (size_t i = 0; i < plan.size(); i++) {
-    const PlanItem &it = plan[i];
-    if (!item_is_block(it)) {
-      rc = apply_item(s, ops, it, engine, u);
-    } else {
-      block_matrix(ops, it, u);
-      rc = apply_block_item(s, it, engine, u);
-      const size_t bytes = u.size() * sizeof(cd);
-      if (c && kept + bytes <= kPlanCacheMatBytes) {
-        c->mats[i] = u;
-        kept += bytes;
-      }
-    }
-    if (rc) return rc;
-  }
+  rc = execute_plan(s, ops, plan, engine, nullptr, c ? &c->mats : nullptr);
+  if (rc) return rc;
   if (c) {
     c->plan = std::move(plan);
     c->n = s->n;
@@ -439,7 +485,8 @@ int collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, int km
       cudaEventCreate(&b);
       cudaEventRecord(a, s->stream);
     }
-    rc = block ? apply_block_item(s, plan[i], engine, u) : apply_item(s, ops, plan[i], engine, u);
+    rc = block ? apply_block_item(s, plan[i], engine, u, nullptr)
+               : apply_item(s, ops, plan[i], engine, u);
     if (timed) {
       cudaEventRecord(b, s->stream);
       ev.push_back(a);
@@ -483,7 +530,7 @@ int qcs_cuda_apply_block(qcs_cuda_state *s, int k, const int *qubits, const doub
     if (seen & (1LL << qubits[j])) return set_error(QCS_CUDA_EINVAL, "repeated qubit %d", qubits[j]);
     seen |= 1LL << qubits[j];
   }
-  return apply_block(s, k, qubits, u, engine, true);
+  return apply_block(s, k, qubits, u, engine, true, nullptr);
 }
 
 int qcs_cuda_plan(const qcs_cuda_op *ops, int count, int num_qubits, int kmax, int *order,

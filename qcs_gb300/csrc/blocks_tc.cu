@@ -91,7 +91,8 @@ struct TcShape {
   static constexpr int OFF_BLK = OFF_COL + kTcM * 8;
   static constexpr int OFF_SQ = OFF_BLK + KA * 8;  // float [slot 4][half][column]
   static constexpr int OFF_EPI = OFF_SQ + kSqSlots * 2 * kTcM * 4;  // LOW mode staging
-  static constexpr int OFF_BAR = OFF_EPI + kTcEpiWarps * 32 * kEpiPitch * 4;
+  static constexpr int OFF_BETA = OFF_EPI + kTcEpiWarps * 32 * kEpiPitch * 4;  // float2[KA]
+  static constexpr int OFF_BAR = OFF_BETA + KA * 8;
   static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
   static constexpr int SMEM = OFF_MISC + 16 + 1024;  // + slack to align the base to 1 KB
   static constexpr int IMG_BYTES = 2 * B_BYTES;
@@ -100,6 +101,9 @@ struct TcShape {
   static_assert(KD % 64 == 0, "K extent must be whole 128-byte swizzle atoms");
   static_assert(TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation size");
 };
+
+// An upload slot: the k = 6 image, then the block's 64 row sums (float2).
+constexpr size_t kImgSlotBytes = TcShape<64>::IMG_BYTES + 64 * 8;
 
 struct TcGeom {
   i64 n_tiles;
@@ -150,7 +154,7 @@ __device__ __forceinline__ TileWalk tile_walk(const TcGeom &g) {
 template <int KA, int MODE>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_block_tc(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
-               int *err) {
+               const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err) {
   using S = TcShape<KA>;
   extern __shared__ uint8_t smem_dyn[];
   const uint32_t raw = smem_u32(smem_dyn);
@@ -187,6 +191,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   {
     uint4 *dst = reinterpret_cast<uint4 *>(sB);
     for (int i = tid; i < S::IMG_BYTES / 16; i += kTcThreads) dst[i] = bimg[i];
+  }
+  // Diffusion fused in front of the block (diffuse_sum != null): the block
+  // reads psi but must act on 2m - psi, m = sum * inv_n; since
+  // U (2m 1 - psi) = 2m (U 1) - U psi, the epilogue writes beta - U psi with
+  // beta[a] = 2m * (row sum a of U), the row sums following the image.
+  float2 *beta = reinterpret_cast<float2 *>(smem + S::OFF_BETA);
+  if (diffuse_sum) {
+    const float tr = (float)(2.0 * (diffuse_sum[0] * inv_n));
+    const float ti = (float)(2.0 * (diffuse_sum[1] * inv_n));
+    const float2 *rows = reinterpret_cast<const float2 *>(bimg + S::IMG_BYTES / 16);
+    for (int i = tid; i < KA; i += kTcThreads) {
+      const float2 r = rows[i];
+      beta[i] = make_float2(tr * r.x - ti * r.y, tr * r.y + ti * r.x);
+    }
   }
   fence_async_shared();  // the block matrix is read by the tensor cores
   if (warp == kTcMmaWarp) {
@@ -385,6 +403,30 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int m = tid;  // TMEM lane = tile column
     const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
     const TileWalk w = tile_walk(g);
+    double sum_re = 0.0, sum_im = 0.0;  // sum of this thread's outputs (sum_out)
+    // Output values of result block c (rows 16c .. 16c+15, re/im
+    // interleaved): the norm-restoring scale, then the fused diffusion's
+    // affine term; their FP32 sum feeds sum_out.
+    auto finish = [&](float (&acc)[32], int c, float scale) {
+      float pr = 0.f, pi = 0.f;
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        float re = acc[2 * q] * scale, im = acc[2 * q + 1] * scale;
+        if (diffuse_sum) {
+          const float2 b = beta[16 * c + q];
+          re = b.x - re;
+          im = b.y - im;
+        }
+        acc[2 * q] = re;
+        acc[2 * q + 1] = im;
+        pr += re;
+        pi += im;
+      }
+      if (sum_out) {
+        sum_re += (double)pr;
+        sum_im += (double)pi;
+      }
+    };
     for (int it = 0; it < w.count; ++it) {
       const i64 tile = w.at(it);
       const int stage = it & 1;
@@ -422,10 +464,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (int c = 0; c < S::N / 32; c++) {
           float acc[32];
           tmem_ld32(tb + 32 * c, acc);
+          finish(acc, c, scale);
 #pragma unroll
           for (int q = 0; q < 16; q++)
             *reinterpret_cast<float2 *>(buf + lane * kEpiPitch + 2 * q) =
-                make_float2(acc[2 * q] * scale, acc[2 * q + 1] * scale);
+                make_float2(acc[2 * q], acc[2 * q + 1]);
           __syncwarp();
 #pragma unroll 4
           for (int j = 0; j < 32; j += 2) {
@@ -440,21 +483,36 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (int c = 0; c < S::N / 32; c++) {
         float acc[32];
         tmem_ld32(tb + 32 * c, acc);
+        finish(acc, c, scale);
         if constexpr (MODE == kPairMode) {
 #pragma unroll
           for (int q = 0; q < 8; q++)
             *reinterpret_cast<float4 *>(dst + blk_off[16 * c + 2 * q]) =
-                make_float4(acc[4 * q] * scale, acc[4 * q + 1] * scale, acc[4 * q + 2] * scale,
-                            acc[4 * q + 3] * scale);
+                make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
         } else {
 #pragma unroll
           for (int q = 0; q < 16; q++)
-            dst[blk_off[16 * c + q]] = make_float2(acc[2 * q] * scale, acc[2 * q + 1] * scale);
+            dst[blk_off[16 * c + q]] = make_float2(acc[2 * q], acc[2 * q + 1]);
         }
       }
       }
       tc_fence_before();
       mbar_arrive(bar(4 + stage));
+    }
+    if (sum_out) {  // one slot per epilogue warp, combined in order on the host side
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sum_re += __shfl_xor_sync(0xffffffffu, sum_re, o);
+        sum_im += __shfl_xor_sync(0xffffffffu, sum_im, o);
+      }
+      if (lane == 0) {
+        ReduceSlot r;
+        r.a = sum_re;
+        r.b = sum_im;
+        r.c = 0.0;
+        r.d = 0.0;
+        sum_out[blockIdx.x * kTcEpiWarps + warp] = r;
+      }
     }
   }
 
@@ -481,7 +539,7 @@ struct TcRing {
 static int ring_init(qcs_cuda_state *s) {
   if (s->tc) return QCS_CUDA_OK;
   TcRing *r = new TcRing();
-  const size_t bytes = (size_t)kImgSlots * TcShape<64>::IMG_BYTES;
+  const size_t bytes = (size_t)kImgSlots * kImgSlotBytes;
   int rc = check_cuda(cudaMallocHost((void **)&r->host, bytes), "cudaMallocHost(block images)");
   if (!rc) rc = check_cuda(cudaMalloc((void **)&r->dev, bytes), "cudaMalloc(block images)");
   for (int i = 0; !rc && i < kImgSlots; i++)
@@ -509,7 +567,8 @@ bool tc_supported(const qcs_cuda_state *s, int k) {
 }
 
 template <int KA, int MODE>
-static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int renorm) {
+static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int renorm,
+                     const double *diffuse_sum, ReduceSlot *sum_out) {
   using S = TcShape<KA>;
   static bool configured = false;
   if (!configured) {
@@ -522,7 +581,7 @@ static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int r
   const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
   prof_begin(s);
   k_block_tc<KA, MODE><<<grid, kTcThreads, S::SMEM, s->stream>>>(
-      (float2 *)s->vec, g, img, renorm, s->d_err);
+      (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err);
   return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
 }
 
@@ -546,7 +605,7 @@ static double unitarity_defect(const double *u, int K) {
 }
 
 int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double *u_in,
-                   bool known_unitary) {
+                   bool known_unitary, const BlockFuse *fuse) {
   int rc = ring_init(s);
   if (rc) return rc;
   TcRing *r = s->tc;
@@ -639,26 +698,51 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
   r->next = (r->next + 1) % kImgSlots;
   rc = check_cuda(cudaEventSynchronize(r->done[slot]), "block image slot");
   if (rc) return rc;
-  const size_t img_bytes = (size_t)TcShape<64>::IMG_BYTES;
-  uint8_t *h = r->host + slot * img_bytes;
-  uint8_t *d = r->dev + slot * img_bytes;
+  uint8_t *h = r->host + slot * kImgSlotBytes;
+  uint8_t *d = r->dev + slot * kImgSlotBytes;
   if (k == 6) make_image<64>(u, h);
   else make_image<32>(u, h);
-  const size_t used = k == 6 ? TcShape<64>::IMG_BYTES : TcShape<32>::IMG_BYTES;
+  size_t used = k == 6 ? TcShape<64>::IMG_BYTES : TcShape<32>::IMG_BYTES;
+  const bool diffuse_in = fuse && fuse->diffuse_in;
+  const bool sum_out = fuse && fuse->sum_out;
+  if (diffuse_in) {  // row sums of the (relabelled) matrix after the image
+    float *rows = reinterpret_cast<float *>(h + used);
+    for (int a = 0; a < KA; a++) {
+      double re = 0.0, im = 0.0;
+      for (int b = 0; b < KA; b++) {
+        re += u[2 * ((size_t)a * KA + b)];
+        im += u[2 * ((size_t)a * KA + b) + 1];
+      }
+      rows[2 * a] = (float)re;
+      rows[2 * a + 1] = (float)im;
+    }
+    used += (size_t)KA * 8;
+    rc = ensure_sum(s);  // m of the state the diffusion acts on
+    if (rc) return rc;
+  }
   rc = copy_h2d(s, d, h, used, "block image upload");
   if (rc) return rc;
   const uint4 *img = reinterpret_cast<const uint4 *>(d);
   const int renorm = (known_unitary || unitarity_defect(u, KA) < 1e-9) ? 1 : 0;
+  const double *dsum = diffuse_in ? s->d_result + 4 : nullptr;
+  ReduceSlot *sout = sum_out ? s->d_partials : nullptr;
   if (k == 6)
-    rc = mode == kLowMode    ? launch_tc<64, kLowMode>(s, g, img, renorm)
-         : mode == kPairMode ? launch_tc<64, kPairMode>(s, g, img, renorm)
-                             : launch_tc<64, kColMode>(s, g, img, renorm);
+    rc = mode == kLowMode    ? launch_tc<64, kLowMode>(s, g, img, renorm, dsum, sout)
+         : mode == kPairMode ? launch_tc<64, kPairMode>(s, g, img, renorm, dsum, sout)
+                             : launch_tc<64, kColMode>(s, g, img, renorm, dsum, sout);
   else
-    rc = mode == kLowMode    ? launch_tc<32, kLowMode>(s, g, img, renorm)
-         : mode == kPairMode ? launch_tc<32, kPairMode>(s, g, img, renorm)
-                             : launch_tc<32, kColMode>(s, g, img, renorm);
+    rc = mode == kLowMode    ? launch_tc<32, kLowMode>(s, g, img, renorm, dsum, sout)
+         : mode == kPairMode ? launch_tc<32, kPairMode>(s, g, img, renorm, dsum, sout)
+                             : launch_tc<32, kColMode>(s, g, img, renorm, dsum, sout);
   if (rc) return rc;
-  return check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
+  rc = check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
+  if (rc) return rc;
+  invalidate_sum(s);
+  if (sum_out) {
+    const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
+    rc = finalize_sum(s, grid * kTcEpiWarps);
+  }
+  return rc;
 }
 
 }  // namespace qcs

@@ -52,6 +52,13 @@ enum KClass {
 struct ProfData;  // per-state event bookkeeping (state.cu)
 struct TcRing;    // tensor-core engine block-matrix uploads (blocks_tc.cu)
 struct PlanCache; // kept fused plan of the last run (blocks.cu)
+// What a tensor-core block also does: take the state through a physical
+// diffusion first (the block reads psi, acts on 2m - psi), and/or leave the
+// sum of its output amplitudes as the state's cached sum.
+struct BlockFuse {
+  bool diffuse_in;
+  bool sum_out;
+};
 void plan_cache_free(qcs_cuda_state *s);
 void tc_release(TcRing *r);
 
@@ -170,6 +177,8 @@ inline int grid_for(i64 work, int threads, const DeviceInfo &d, int per_sm) {
 
 // ---- cross-file entry points ------------------------------------------------
 void invalidate_sum(qcs_cuda_state *s);
+int ensure_sum(qcs_cuda_state *s);                  // readout.cu
+int finalize_sum(qcs_cuda_state *s, int nslots);    // readout.cu
 int ensure_sample_scratch(qcs_cuda_state *s, int shots);
 
 }  // namespace qcs

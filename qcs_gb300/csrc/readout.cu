@@ -495,6 +495,24 @@ int diffusion(qcs_cuda_state *s) {
 
 int norm_sq(qcs_cuda_state *s, double *out) { return reduce(s, OP_NORM, 0, out, 1); }
 
+// The cached amplitude sum, computed now unless it is valid.
+int ensure_sum(qcs_cuda_state *s) {
+  if (s->sum_valid) return QCS_CUDA_OK;
+  int rc = reduce(s, OP_SUM, 0, nullptr, 0);
+  if (!rc) s->sum_valid = 1;
+  return rc;
+}
+
+// A kernel left per-part sums of the new amplitudes in d_partials[0..nslots):
+// combine them (fixed order) into the cached sum.
+int finalize_sum(qcs_cuda_state *s, int nslots) {
+  prof_begin(s);
+  k_finalize<<<1, 32, 0, s->stream>>>(s->d_partials, nslots, s->d_result + 4);
+  int rc = launched(s, KC_OTHER, nslots * 32.0, "sum finalize");
+  if (!rc) s->sum_valid = 1;
+  return rc;
+}
+
 }  // namespace qcs
 
 using namespace qcs;

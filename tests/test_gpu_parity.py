@@ -468,6 +468,34 @@ def test_kept_plan_replays_identically(engine, k):
         assert not np.array_equal(a, c)
 
 
+def test_grover_rounds_fuse_diffusion_into_tensor_core_blocks():
+    """QFT + rounds of (Hadamard layer, phase flip, diffusion), fused at width
+    6 on a state the tensor cores take: every diffusion but the last runs
+    inside the following block, and the block before each flip leaves the
+    sum the diffusion needs, so no separate reduction or diffusion sweep
+    runs; the state still matches the FP64 oracle."""
+    n = 16
+    w = W.grover_workload(n, 8, iterations=8)
+    full = W.basis_gates(n, w.basis)
+    full.extend(w.qft)
+    full.extend(w.rounds)
+    with capi.State(n, capi.C64) as s, oracle_state(n, full) as o:
+        s.profile(True)
+        s.run(full, fusion_k=6)
+        prof = s.profile_read()
+        s.profile(False)
+        a, b = s.amplitudes(), o.amplitudes()
+        assert infidelity(a, b) < 1e-6
+        pm = o.probability(w.marked)
+        assert abs(s.probability(w.marked) - pm) < 1e-3 * pm
+    assert prof["diffuse"][0] == 1        # the last round's, with no block after it
+    assert "reduce" not in prof           # sums come from the blocks' epilogues
+    with capi.State(n, capi.C64) as s, oracle_state(n, w.search) as o:
+        s.run(w.search, fusion_k=6)
+        assert s.argmax() == o.argmax() == w.marked
+        assert infidelity(s.amplitudes(), o.amplitudes()) < 1e-6
+
+
 # ---- full size: size-independent properties ------------------------------------------
 
 def _inverse(g: W.GateList) -> W.GateList:
