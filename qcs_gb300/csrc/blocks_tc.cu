@@ -151,7 +151,9 @@ __device__ __forceinline__ TileWalk tile_walk(const TcGeom &g) {
 
 // In kColMode and kPairMode a producer thread keeps one column (tile row
 // m = p % 128) and consecutive threads take consecutive columns.
-template <int KA, int MODE>
+// FUSED: the launch may fuse a diffusion in front of the block and/or leave
+// the sum of its outputs (the plain instantiation carries neither cost).
+template <int KA, int MODE, bool FUSED>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_block_tc(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
                const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err) {
@@ -197,7 +199,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // U (2m 1 - psi) = 2m (U 1) - U psi, the epilogue writes beta - U psi with
   // beta[a] = 2m * (row sum a of U), the row sums following the image.
   float2 *beta = reinterpret_cast<float2 *>(smem + S::OFF_BETA);
-  if (diffuse_sum) {
+  if (FUSED && diffuse_sum) {
     const float tr = (float)(2.0 * (diffuse_sum[0] * inv_n));
     const float ti = (float)(2.0 * (diffuse_sum[1] * inv_n));
     const float2 *rows = reinterpret_cast<const float2 *>(bimg + S::IMG_BYTES / 16);
@@ -408,23 +410,28 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // interleaved): the norm-restoring scale, then the fused diffusion's
     // affine term; their FP32 sum feeds sum_out.
     auto finish = [&](float (&acc)[32], int c, float scale) {
-      float pr = 0.f, pi = 0.f;
+      if constexpr (!FUSED) {
 #pragma unroll
-      for (int q = 0; q < 16; q++) {
-        float re = acc[2 * q] * scale, im = acc[2 * q + 1] * scale;
-        if (diffuse_sum) {
-          const float2 b = beta[16 * c + q];
-          re = b.x - re;
-          im = b.y - im;
+        for (int q = 0; q < 32; q++) acc[q] *= scale;
+      } else {
+        float pr = 0.f, pi = 0.f;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          float re = acc[2 * q] * scale, im = acc[2 * q + 1] * scale;
+          if (diffuse_sum) {
+            const float2 b = beta[16 * c + q];
+            re = b.x - re;
+            im = b.y - im;
+          }
+          acc[2 * q] = re;
+          acc[2 * q + 1] = im;
+          pr += re;
+          pi += im;
         }
-        acc[2 * q] = re;
-        acc[2 * q + 1] = im;
-        pr += re;
-        pi += im;
-      }
-      if (sum_out) {
-        sum_re += (double)pr;
-        sum_im += (double)pi;
+        if (sum_out) {
+          sum_re += (double)pr;
+          sum_im += (double)pi;
+        }
       }
     };
     for (int it = 0; it < w.count; ++it) {
@@ -499,7 +506,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_fence_before();
       mbar_arrive(bar(4 + stage));
     }
-    if (sum_out) {  // one slot per epilogue warp, combined in order on the host side
+    if (FUSED && sum_out) {  // one slot per epilogue warp, combined in order afterwards
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         sum_re += __shfl_xor_sync(0xffffffffu, sum_re, o);
@@ -572,16 +579,24 @@ static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int r
   using S = TcShape<KA>;
   static bool configured = false;
   if (!configured) {
-    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc<KA, MODE>,
+    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc<KA, MODE, false>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM),
                         "cudaFuncSetAttribute(tcgen05 block)");
+    if (!rc)
+      rc = check_cuda(cudaFuncSetAttribute(k_block_tc<KA, MODE, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM),
+                      "cudaFuncSetAttribute(tcgen05 block, fused)");
     if (rc) return rc;
     configured = true;
   }
   const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
   prof_begin(s);
-  k_block_tc<KA, MODE><<<grid, kTcThreads, S::SMEM, s->stream>>>(
-      (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err);
+  if (diffuse_sum || sum_out)
+    k_block_tc<KA, MODE, true><<<grid, kTcThreads, S::SMEM, s->stream>>>(
+        (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err);
+  else
+    k_block_tc<KA, MODE, false><<<grid, kTcThreads, S::SMEM, s->stream>>>(
+        (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err);
   return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
 }
 
