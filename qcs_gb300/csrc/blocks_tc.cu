@@ -600,23 +600,46 @@ static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int r
   return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
 }
 
-// Largest |(U^H U - I)_ij|: unitary blocks get the per-column norm restore.
-static double unitarity_defect(const double *u, int K) {
-  double worst = 0.0;
-  for (int a = 0; a < K; a++)
-    for (int b = 0; b < K; b++) {
+// Whether U is unitary (to FP64 rounding): unitary blocks get the
+// per-column norm restore.  Checked as |U^H U v - v| <= 1e-9 |v| for two
+// fixed pseudo-random vectors v, O(K^2) instead of the O(K^3) of forming
+// U^H U: a non-unitary U has U^H U - I != 0, which a random v lies in the
+// null space of with probability zero.
+static bool is_unitary(const double *u, int K) {
+  std::vector<double> v(2 * K), w(2 * K), x(2 * K);
+  unsigned long long st = 0x9E3779B97F4A7C15ULL;
+  for (int trial = 0; trial < 2; trial++) {
+    double vn = 0.0;
+    for (int i = 0; i < 2 * K; i++) {
+      st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+      v[i] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+      vn += v[i] * v[i];
+    }
+    for (int r = 0; r < K; r++) {  // w = U v
+      double re = 0.0, im = 0.0;
+      for (int c = 0; c < K; c++) {
+        const double ur = u[2 * (r * K + c)], ui = u[2 * (r * K + c) + 1];
+        re += ur * v[2 * c] - ui * v[2 * c + 1];
+        im += ur * v[2 * c + 1] + ui * v[2 * c];
+      }
+      w[2 * r] = re;
+      w[2 * r + 1] = im;
+    }
+    for (int c = 0; c < K; c++) {  // x = U^H w
       double re = 0.0, im = 0.0;
       for (int r = 0; r < K; r++) {
-        const double ar = u[2 * (r * K + a)], ai = -u[2 * (r * K + a) + 1];
-        const double br = u[2 * (r * K + b)], bi = u[2 * (r * K + b) + 1];
-        re += ar * br - ai * bi;
-        im += ar * bi + ai * br;
+        const double ur = u[2 * (r * K + c)], ui = -u[2 * (r * K + c) + 1];
+        re += ur * w[2 * r] - ui * w[2 * r + 1];
+        im += ur * w[2 * r + 1] + ui * w[2 * r];
       }
-      if (a == b) re -= 1.0;
-      const double d = fabs(re) + fabs(im);
-      if (d > worst) worst = d;
+      x[2 * c] = re;
+      x[2 * c + 1] = im;
     }
-  return worst;
+    double dn = 0.0;
+    for (int i = 0; i < 2 * K; i++) dn += (x[i] - v[i]) * (x[i] - v[i]);
+    if (!(dn <= 1e-18 * vn)) return false;
+  }
+  return true;
 }
 
 int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double *u_in,
@@ -738,7 +761,7 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
   rc = copy_h2d(s, d, h, used, "block image upload");
   if (rc) return rc;
   const uint4 *img = reinterpret_cast<const uint4 *>(d);
-  const int renorm = (known_unitary || unitarity_defect(u, KA) < 1e-9) ? 1 : 0;
+  const int renorm = (known_unitary || is_unitary(u, KA)) ? 1 : 0;
   const double *dsum = diffuse_in ? s->d_result + 4 : nullptr;
   ReduceSlot *sout = sum_out ? s->d_partials : nullptr;
   if (k == 6)

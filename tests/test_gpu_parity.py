@@ -387,6 +387,26 @@ def test_auto_engine_widens_four_qubit_blocks():
         assert infidelity(s.amplitudes(), o.amplitudes()) < 1e-6
 
 
+def test_tensor_cores_apply_non_unitary_matrices_as_given():
+    """A matrix that is not unitary (scaled, or a projector) passed to
+    qcs_cuda_apply_block is applied as the plain linear map: the per-column
+    norm restore is only for unitary blocks."""
+    n = 15
+    rng = np.random.default_rng(55)
+    u, _ = np.linalg.qr(rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64)))
+    proj = np.diag([1.0 if i % 3 else 0.0 for i in range(64)]).astype(complex)
+    for m in (0.5 * u, proj, u @ proj):
+        init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        init /= np.linalg.norm(init)
+        with capi.State(n, capi.C64) as s, O.OracleState(n) as o:
+            s.set_amplitudes(init)
+            o.set_amplitudes(init)
+            s.apply_block([1, 4, 6, 8, 11, 13], m, capi.FUSE_TENSOR)
+            o.apply_block([1, 4, 6, 8, 11, 13], m)
+            a, b = s.amplitudes(), o.amplitudes()
+            assert np.max(np.abs(a - b)) < TC_ATOL
+
+
 def test_tensor_cores_preserve_the_norm_over_many_blocks():
     """100 random 6-qubit unitaries: FP32 accumulation in the tensor cores
     rounds toward zero; the per-column norm restore must keep the state's
