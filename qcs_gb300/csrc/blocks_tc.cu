@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // Output values of result block c (rows 16c .. 16c+15, re/im
     // interleaved): the norm-restoring scale, then the fused diffusion's
     // affine term; their FP32 sum feeds sum_out.
-    auto finish = [&](float (&acc)[32], int c, float scale) {
+    auto finish = [&](float *acc, int c, float scale) {
       if constexpr (!FUSED) {
 #pragma unroll
         for (int q = 0; q < 32; q++) acc[q] *= scale;
@@ -444,14 +444,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_fence_after();
       const uint32_t tb = tmem + lane_addr + (uint32_t)(stage * S::N);
       float scale = 1.f;
+      // TMEM is read 64 columns per instruction: each tcgen05.ld waits for
+      // its data, and the epilogue is the slower side of the pipeline when
+      // the loads are contiguous
       if (renorm) {
         float out = 0.f;
 #pragma unroll 1
-        for (int c = 0; c < S::N / 32; c++) {
-          float acc[32];
-          tmem_ld32(tb + 32 * c, acc);
+        for (int cc = 0; cc < S::N / 64; cc++) {
+          float acc[64];
+          tmem_ld64(tb + 64 * cc, acc);
 #pragma unroll
-          for (int q = 0; q < 32; q++) out += acc[q] * acc[q];
+          for (int q = 0; q < 64; q++) out += acc[q] * acc[q];
         }
         const float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
         const float in = sq[m] + sq[kTcM + m];
@@ -468,38 +471,49 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         float *buf = epi + warp * 32 * kEpiPitch;
         const int half = lane >> 4, row = lane & 15;
 #pragma unroll 1
-        for (int c = 0; c < S::N / 32; c++) {
-          float acc[32];
-          tmem_ld32(tb + 32 * c, acc);
-          finish(acc, c, scale);
+        for (int cc = 0; cc < S::N / 64; cc++) {
+          float acc[64];
+          tmem_ld64(tb + 64 * cc, acc);
 #pragma unroll
-          for (int q = 0; q < 16; q++)
-            *reinterpret_cast<float2 *>(buf + lane * kEpiPitch + 2 * q) =
-                make_float2(acc[2 * q], acc[2 * q + 1]);
-          __syncwarp();
+          for (int h = 0; h < 2; h++) {
+            const int c = 2 * cc + h;
+            float *a = acc + 32 * h;
+            finish(a, c, scale);
+#pragma unroll
+            for (int q = 0; q < 16; q++)
+              *reinterpret_cast<float2 *>(buf + lane * kEpiPitch + 2 * q) =
+                  make_float2(a[2 * q], a[2 * q + 1]);
+            __syncwarp();
 #pragma unroll 4
-          for (int j = 0; j < 32; j += 2) {
-            const float2 val = *reinterpret_cast<const float2 *>(buf + (j + half) * kEpiPitch + 2 * row);
-            v[base + col_off[warp * 32 + j + half] + 16 * c + row] = val;
+            for (int j = 0; j < 32; j += 2) {
+              const float2 val =
+                  *reinterpret_cast<const float2 *>(buf + (j + half) * kEpiPitch + 2 * row);
+              v[base + col_off[warp * 32 + j + half] + 16 * c + row] = val;
+            }
+            __syncwarp();
           }
-          __syncwarp();
         }
       } else {
       float2 *dst = v + base + col_off[m];
 #pragma unroll 1
-      for (int c = 0; c < S::N / 32; c++) {
-        float acc[32];
-        tmem_ld32(tb + 32 * c, acc);
-        finish(acc, c, scale);
-        if constexpr (MODE == kPairMode) {
+      for (int cc = 0; cc < S::N / 64; cc++) {
+        float acc[64];
+        tmem_ld64(tb + 64 * cc, acc);
 #pragma unroll
-          for (int q = 0; q < 8; q++)
-            *reinterpret_cast<float4 *>(dst + blk_off[16 * c + 2 * q]) =
-                make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
-        } else {
+        for (int h = 0; h < 2; h++) {
+          const int c = 2 * cc + h;
+          float *a = acc + 32 * h;
+          finish(a, c, scale);
+          if constexpr (MODE == kPairMode) {
 #pragma unroll
-          for (int q = 0; q < 16; q++)
-            dst[blk_off[16 * c + q]] = make_float2(acc[2 * q], acc[2 * q + 1]);
+            for (int q = 0; q < 8; q++)
+              *reinterpret_cast<float4 *>(dst + blk_off[16 * c + 2 * q]) =
+                  make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 16; q++)
+              dst[blk_off[16 * c + q]] = make_float2(a[2 * q], a[2 * q + 1]);
+          }
         }
       }
       }
