@@ -313,9 +313,17 @@ struct PlanCache {
   unsigned long long cm_gen = 0;
   std::vector<PlanItem> plan;
   std::vector<std::vector<cd>> mats;  // per item: the block matrix, or empty
+  std::vector<TcResident *> res;      // per item: a resident tensor-core block, or null
+  void clear_blocks() {
+    for (TcResident *r : res) tc_free_resident(r);
+    res.clear();
+    mats.clear();
+  }
+  ~PlanCache() { clear_blocks(); }
 };
 
-// Block matrices are kept while their total stays under this many bytes.
+// Block matrices (host) and resident tensor-core images (device) are kept
+// while their total stays under this many bytes.
 constexpr size_t kPlanCacheMatBytes = 64u << 20;
 
 void plan_cache_free(qcs_cuda_state *s) {
@@ -357,9 +365,8 @@ static bool item_is_op(const qcs_cuda_op *ops, const PlanItem &it, int kind) {
 // matrices come from `use_mats` where present, else are formed here and,
 // within the budget, kept in `store_mats`.
 static int execute_plan(qcs_cuda_state *s, const qcs_cuda_op *ops,
-                        const std::vector<PlanItem> &plan, int engine,
-                        const std::vector<std::vector<cd>> *use_mats,
-                        std::vector<std::vector<cd>> *store_mats) {
+                        const std::vector<PlanItem> &plan, int engine, PlanCache *use,
+                        PlanCache *store) {
   auto on_tc = [&](const PlanItem &it) {
     return item_is_block(it) && it.qubits.size() >= 2 &&
            block_on_tensor_cores(s, (int)it.qubits.size(), engine);
@@ -387,15 +394,38 @@ static int execute_plan(qcs_cuda_state *s, const qcs_cuda_op *ops,
       }
       diffusion_pending = false;
       const BlockFuse *fp = (f.diffuse_in || f.sum_out) ? &f : nullptr;
-      if (use_mats && !(*use_mats)[i].empty()) {
-        rc = apply_block_item(s, it, engine, (*use_mats)[i], fp);
+      if (use && use->res[i]) {
+        rc = tc_launch_resident(s, use->res[i], fp);
+      } else if (use && !use->mats[i].empty()) {
+        rc = apply_block_item(s, it, engine, use->mats[i], fp);
       } else {
         block_matrix(ops, it, u);
-        rc = apply_block_item(s, it, engine, u, fp);
         const size_t bytes = u.size() * sizeof(cd);
-        if (store_mats && kept + bytes <= kPlanCacheMatBytes) {
-          (*store_mats)[i] = u;
-          kept += bytes;
+        if (store && kept + bytes <= kPlanCacheMatBytes && on_tc(it)) {
+          // keep it on the device, prepared (widened to 5 qubits for k < 5)
+          const int kb = (int)it.qubits.size();
+          TcResident *r = nullptr;
+          if (tc_supported(s, kb) && (engine == QCS_FUSE_TENSOR || kb > 4)) {
+            rc = tc_make_resident(s, kb, it.qubits.data(),
+                                  reinterpret_cast<const double *>(u.data()), true, &r);
+          } else {
+            int q5[5];
+            std::vector<double> u5;
+            widen_to_5(s, kb, it.qubits.data(), reinterpret_cast<const double *>(u.data()), q5,
+                       u5);
+            rc = tc_make_resident(s, 5, q5, u5.data(), true, &r);
+          }
+          if (!rc) {
+            store->res[i] = r;
+            kept += tc_resident_bytes(r);
+            rc = tc_launch_resident(s, r, fp);
+          }
+        } else {
+          rc = apply_block_item(s, it, engine, u, fp);
+          if (store && kept + bytes <= kPlanCacheMatBytes) {
+            store->mats[i] = u;
+            kept += bytes;
+          }
         }
       }
     }
@@ -423,7 +453,7 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
   const unsigned long long gen = learned ? costmodel_generation(s->cm) : 0;
   const bool use_cache = !(opt->flags & QCS_RUN_NO_PLAN_CACHE);
   if (use_cache && plan_cache_hit(s->plans, ops, count, s->n, k, engine, part, cm, gen))
-    return execute_plan(s, ops, s->plans->plan, engine, &s->plans->mats, nullptr);
+    return execute_plan(s, ops, s->plans->plan, engine, s->plans, nullptr);
   std::vector<PlanItem> plan;
   if (learned) {
     const bool simt_only = engine == QCS_FUSE_SIMT;
@@ -442,9 +472,11 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
     c = s->plans;
     c->n = -1;  // invalid until the run completes
     c->ops.assign(ops, ops + count);
+    c->clear_blocks();
     c->mats.assign(plan.size(), std::vector<cd>());
+    c->res.assign(plan.size(), nullptr);
   }
-  rc = execute_plan(s, ops, plan, engine, nullptr, c ? &c->mats : nullptr);
+  rc = execute_plan(s, ops, plan, engine, nullptr, c);
   if (rc) return rc;
   if (c) {
     c->plan = std::move(plan);

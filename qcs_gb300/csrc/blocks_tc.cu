@@ -656,11 +656,20 @@ static bool is_unitary(const double *u, int K) {
   return true;
 }
 
-int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double *u_in,
-                   bool known_unitary, const BlockFuse *fuse) {
-  int rc = ring_init(s);
-  if (rc) return rc;
-  TcRing *r = s->tc;
+// A block made ready for the tensor cores: ascending qubits (the matrix
+// relabelled to match), geometry, access mode, whether the norm is restored,
+// and the image: split-BF16 B, then the matrix's row sums (float2) that a
+// fused diffusion needs.
+struct TcResident {
+  int k = 0, mode = 0, renorm = 0;
+  size_t image_bytes = 0;
+  TcGeom g;
+  std::vector<uint8_t> image;  // host copy
+  uint8_t *dev = nullptr;      // device copy (resident blocks only)
+};
+
+static void tc_prepare(const qcs_cuda_state *s, int k, const int *qubits_in, const double *u_in,
+                       bool known_unitary, TcResident &out) {
   const int KA = 1 << k;
   // Ascending qubits (block bit j = j-th smallest qubit), the matrix relabelled
   // to match: new index a' has bit j where the old index has bit order[j].
@@ -692,7 +701,7 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
     u = u_perm.data();
   }
   // geometry
-  TcGeom g;
+  TcGeom &g = out.g;
   memset(&g, 0, sizeof(g));
   std::vector<int> role(s->n, -1);  // >= 0 block bit, -2 column, -1 free
   for (int j = 0; j < k; j++) role[qubits[j]] = j;
@@ -744,50 +753,47 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
   }
   bool low = true;  // the block is exactly qubits 0..k-1
   for (int j = 0; j < k; j++) low = low && qubits[j] == j;
-  const int mode = low ? kLowMode : (qubits[0] == 0 ? kPairMode : kColMode);
-  // block-matrix image through the pinned ring
-  const int slot = r->next;
-  r->next = (r->next + 1) % kImgSlots;
-  rc = check_cuda(cudaEventSynchronize(r->done[slot]), "block image slot");
-  if (rc) return rc;
-  uint8_t *h = r->host + slot * kImgSlotBytes;
-  uint8_t *d = r->dev + slot * kImgSlotBytes;
-  if (k == 6) make_image<64>(u, h);
-  else make_image<32>(u, h);
-  size_t used = k == 6 ? TcShape<64>::IMG_BYTES : TcShape<32>::IMG_BYTES;
+  out.k = k;
+  out.mode = low ? kLowMode : (qubits[0] == 0 ? kPairMode : kColMode);
+  out.renorm = (known_unitary || is_unitary(u, KA)) ? 1 : 0;
+  const size_t img = k == 6 ? TcShape<64>::IMG_BYTES : TcShape<32>::IMG_BYTES;
+  out.image_bytes = img + (size_t)KA * 8;
+  out.image.assign(out.image_bytes, 0);
+  if (k == 6) make_image<64>(u, out.image.data());
+  else make_image<32>(u, out.image.data());
+  float *rows = reinterpret_cast<float *>(out.image.data() + img);
+  for (int a = 0; a < KA; a++) {
+    double re = 0.0, im = 0.0;
+    for (int b = 0; b < KA; b++) {
+      re += u[2 * ((size_t)a * KA + b)];
+      im += u[2 * ((size_t)a * KA + b) + 1];
+    }
+    rows[2 * a] = (float)re;
+    rows[2 * a + 1] = (float)im;
+  }
+}
+
+// Launches a prepared block whose image is at `img` on the device.
+static int tc_launch(qcs_cuda_state *s, const TcResident &b, const uint4 *img,
+                     const BlockFuse *fuse) {
   const bool diffuse_in = fuse && fuse->diffuse_in;
   const bool sum_out = fuse && fuse->sum_out;
-  if (diffuse_in) {  // row sums of the (relabelled) matrix after the image
-    float *rows = reinterpret_cast<float *>(h + used);
-    for (int a = 0; a < KA; a++) {
-      double re = 0.0, im = 0.0;
-      for (int b = 0; b < KA; b++) {
-        re += u[2 * ((size_t)a * KA + b)];
-        im += u[2 * ((size_t)a * KA + b) + 1];
-      }
-      rows[2 * a] = (float)re;
-      rows[2 * a + 1] = (float)im;
-    }
-    used += (size_t)KA * 8;
+  int rc = QCS_CUDA_OK;
+  if (diffuse_in) {
     rc = ensure_sum(s);  // m of the state the diffusion acts on
     if (rc) return rc;
   }
-  rc = copy_h2d(s, d, h, used, "block image upload");
-  if (rc) return rc;
-  const uint4 *img = reinterpret_cast<const uint4 *>(d);
-  const int renorm = (known_unitary || is_unitary(u, KA)) ? 1 : 0;
   const double *dsum = diffuse_in ? s->d_result + 4 : nullptr;
   ReduceSlot *sout = sum_out ? s->d_partials : nullptr;
-  if (k == 6)
-    rc = mode == kLowMode    ? launch_tc<64, kLowMode>(s, g, img, renorm, dsum, sout)
-         : mode == kPairMode ? launch_tc<64, kPairMode>(s, g, img, renorm, dsum, sout)
-                             : launch_tc<64, kColMode>(s, g, img, renorm, dsum, sout);
+  const TcGeom &g = b.g;
+  if (b.k == 6)
+    rc = b.mode == kLowMode    ? launch_tc<64, kLowMode>(s, g, img, b.renorm, dsum, sout)
+         : b.mode == kPairMode ? launch_tc<64, kPairMode>(s, g, img, b.renorm, dsum, sout)
+                               : launch_tc<64, kColMode>(s, g, img, b.renorm, dsum, sout);
   else
-    rc = mode == kLowMode    ? launch_tc<32, kLowMode>(s, g, img, renorm, dsum, sout)
-         : mode == kPairMode ? launch_tc<32, kPairMode>(s, g, img, renorm, dsum, sout)
-                             : launch_tc<32, kColMode>(s, g, img, renorm, dsum, sout);
-  if (rc) return rc;
-  rc = check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
+    rc = b.mode == kLowMode    ? launch_tc<32, kLowMode>(s, g, img, b.renorm, dsum, sout)
+         : b.mode == kPairMode ? launch_tc<32, kPairMode>(s, g, img, b.renorm, dsum, sout)
+                               : launch_tc<32, kColMode>(s, g, img, b.renorm, dsum, sout);
   if (rc) return rc;
   invalidate_sum(s);
   if (sum_out) {
@@ -795,6 +801,71 @@ int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits_in, const double 
     rc = finalize_sum(s, grid * kTcEpiWarps);
   }
   return rc;
+}
+
+int apply_block_tc(qcs_cuda_state *s, int k, const int *qubits, const double *u,
+                   bool known_unitary, const BlockFuse *fuse) {
+  int rc = ring_init(s);
+  if (rc) return rc;
+  TcRing *r = s->tc;
+  TcResident b;
+  tc_prepare(s, k, qubits, u, known_unitary, b);
+  // the image through the pinned ring
+  const int slot = r->next;
+  r->next = (r->next + 1) % kImgSlots;
+  rc = check_cuda(cudaEventSynchronize(r->done[slot]), "block image slot");
+  if (rc) return rc;
+  uint8_t *h = r->host + slot * kImgSlotBytes;
+  uint8_t *d = r->dev + slot * kImgSlotBytes;
+  memcpy(h, b.image.data(), b.image_bytes);
+  rc = copy_h2d(s, d, h, b.image_bytes, "block image upload");
+  if (rc) return rc;
+  rc = tc_launch(s, b, reinterpret_cast<const uint4 *>(d), fuse);
+  if (rc) return rc;
+  return check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
+}
+
+// Resident blocks: prepared once, image kept on the device, launched with no
+// host-to-device traffic (kept plans).
+int tc_make_resident(qcs_cuda_state *s, int k, const int *qubits, const double *u,
+                     bool known_unitary, TcResident **out) {
+  int rc = ring_init(s);
+  if (rc) return rc;
+  TcResident *b = new TcResident();
+  tc_prepare(s, k, qubits, u, known_unitary, *b);
+  rc = check_cuda(cudaMalloc((void **)&b->dev, b->image_bytes), "cudaMalloc(block image)");
+  if (!rc) {  // through the pinned ring, so that the copy stays asynchronous
+    TcRing *r = s->tc;
+    const int slot = r->next;
+    r->next = (r->next + 1) % kImgSlots;
+    rc = check_cuda(cudaEventSynchronize(r->done[slot]), "block image slot");
+    if (!rc) {
+      memcpy(r->host + slot * kImgSlotBytes, b->image.data(), b->image_bytes);
+      rc = copy_h2d(s, b->dev, r->host + slot * kImgSlotBytes, b->image_bytes,
+                    "block image upload");
+    }
+    if (!rc) rc = check_cuda(cudaEventRecord(r->done[slot], s->stream), "block image event");
+  }
+  if (rc) {
+    tc_free_resident(b);
+    return rc;
+  }
+  b->image.clear();
+  b->image.shrink_to_fit();
+  *out = b;
+  return QCS_CUDA_OK;
+}
+
+int tc_launch_resident(qcs_cuda_state *s, const TcResident *b, const BlockFuse *fuse) {
+  return tc_launch(s, *b, reinterpret_cast<const uint4 *>(b->dev), fuse);
+}
+
+size_t tc_resident_bytes(const TcResident *b) { return b->image_bytes; }
+
+void tc_free_resident(TcResident *b) {
+  if (!b) return;
+  if (b->dev) cudaFree(b->dev);
+  delete b;
 }
 
 }  // namespace qcs

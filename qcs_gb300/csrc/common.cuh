@@ -52,6 +52,7 @@ enum KClass {
 struct ProfData;  // per-state event bookkeeping (state.cu)
 struct TcRing;    // tensor-core engine block-matrix uploads (blocks_tc.cu)
 struct PlanCache; // kept fused plan of the last run (blocks.cu)
+struct TcResident;  // a tensor-core block with its image on the device (blocks_tc.cu)
 // What a tensor-core block also does: take the state through a physical
 // diffusion first (the block reads psi, acts on 2m - psi), and/or leave the
 // sum of its output amplitudes as the state's cached sum.
@@ -59,6 +60,12 @@ struct BlockFuse {
   bool diffuse_in;
   bool sum_out;
 };
+// Tensor-core blocks kept with a plan (blocks_tc.cu).
+int tc_make_resident(qcs_cuda_state *s, int k, const int *qubits, const double *u,
+                     bool known_unitary, TcResident **out);
+int tc_launch_resident(qcs_cuda_state *s, const TcResident *b, const BlockFuse *fuse);
+size_t tc_resident_bytes(const TcResident *b);
+void tc_free_resident(TcResident *b);
 void plan_cache_free(qcs_cuda_state *s);
 void tc_release(TcRing *r);
 
