@@ -314,7 +314,9 @@ def test_transfer_counters():
         u, _ = np.linalg.qr(np.random.default_rng(1).normal(size=(64, 64)) + 0j)
         s.apply_block(list(range(6)), u, capi.FUSE_TENSOR)
         h4, _ = s.transfer_bytes()
-        assert h4 - h3 == 2 * 128 * 128 * 2  # bf16 hi + lo image of the 128 x 128 real form
+        # bf16 hi + lo image of the 128 x 128 real form, then the 64 complex
+        # row sums (float2) a fused diffusion reads
+        assert h4 - h3 == 2 * 128 * 128 * 2 + 64 * 8
         draws = np.linspace(0.01, 0.99, 100)
         s.sample(draws)
         h5, d5 = s.transfer_bytes()

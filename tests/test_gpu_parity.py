@@ -462,20 +462,28 @@ def test_fused_with_grover_barriers():
         assert s.argmax() == o.argmax() == w.marked
 
 
-@pytest.mark.parametrize("engine,k", [(capi.FUSE_SIMT, 5), (capi.FUSE_TENSOR, 6)])
+@pytest.mark.parametrize("engine,k", [(capi.FUSE_SIMT, 5), (capi.FUSE_TENSOR, 6),
+                                      (capi.FUSE_AUTO, 4)])
 def test_kept_plan_replays_identically(engine, k):
     """A second run of the same op list reuses the kept plan and block
     matrices and gives the same amplitudes, bit for bit, as planning afresh;
-    a list with one angle changed is planned afresh."""
+    a list with one angle changed is planned afresh.  Tensor-core blocks of a
+    kept plan stay on the device, so a replay uploads no block images."""
     n = 16
     g = W.mixed_circuit(n, 12, 5)
     with capi.State(n, capi.C64) as s:
+        h0, _ = s.transfer_bytes()
         s.run(g, fusion_k=k, engine=engine, plan_cache=False)
+        h1, _ = s.transfer_bytes()
         a = s.amplitudes()
         for _ in range(2):
             s.set_basis(0)
+            h2, _ = s.transfer_bytes()
             s.run(g, fusion_k=k, engine=engine)
+            h3, _ = s.transfer_bytes()
             assert np.array_equal(s.amplitudes(), a)
+        if engine != capi.FUSE_SIMT:  # the last replay moved no block image
+            assert h3 - h2 < min(h1 - h0, 2 * 64 * 64 * 2)  # one 5-qubit image
         ops = g.ops().copy()
         i = int(np.nonzero(np.isin(ops["kind"], (W.RX, W.RY, W.RZ, W.P)))[0][0])
         ops["angle"][i] += 0.5
