@@ -456,6 +456,11 @@ TC_PLACEMENTS = {"block_tc6_low": lambda n: list(range(6)),
                  "block_tc6_mid": lambda n: list(range(6, 12)),
                  "block_tc6_high": lambda n: list(range(n - 6, n)),
                  "block_tc6_spread": lambda n: [1, 6, 11, 16, 21, 26]}
+TC7_PLACEMENTS = {"block_tc7_low": lambda n: list(range(7)),
+                  "block_tc7_q0": lambda n: [0, 4, 8, 12, 16, 20, 24],
+                  "block_tc7_mid": lambda n: list(range(7, 14)),
+                  "block_tc7_high": lambda n: list(range(n - 7, n)),
+                  "block_tc7_spread": lambda n: [1, 5, 9, 13, 17, 21, 25]}
 
 
 def run_sweeps(args, dist):
@@ -475,6 +480,7 @@ def run_sweeps(args, dist):
     with capi.State(n, capi.C64) as s:
         s.run(W.brick_circuit(n, 1, args.seed))  # a generic dense state (plain kernels)
         s.synchronize()
+        u7, _ = np.linalg.qr(rng.normal(size=(128, 128)) + 1j * rng.normal(size=(128, 128)))
         u6, _ = np.linalg.qr(rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64)))
         u5, _ = np.linalg.qr(rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32)))
         u4, _ = np.linalg.qr(rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16)))
@@ -501,8 +507,12 @@ def run_sweeps(args, dist):
                                                   capi.FUSE_TENSOR), 2 * Ns),
             "block_tc5": (lambda i: s.apply_block([(i + 3 * j) % n for j in range(5)], u5,
                                                   capi.FUSE_TENSOR), 2 * Ns),
+            "block_tc7": (lambda i: s.apply_block([(i + 3 * j) % n for j in range(7)], u7,
+                                                  capi.FUSE_TENSOR), 2 * Ns),
             **{name: ((lambda i, q=place(n): s.apply_block(q, u6, capi.FUSE_TENSOR)), 2 * Ns)
                for name, place in TC_PLACEMENTS.items()},
+            **{name: ((lambda i, q=place(n): s.apply_block(q, u7, capi.FUSE_TENSOR)), 2 * Ns)
+               for name, place in TC7_PLACEMENTS.items()},
             "norm": (lambda i: s.norm_sq(), Ns),
             "argmax": (lambda i: s.argmax(), Ns),
             "diffuse": (lambda i: s.diffusion(), 2 * Ns),

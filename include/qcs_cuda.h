@@ -99,7 +99,7 @@ typedef struct qcs_cuda_run_options {
 
 #define QCS_FUSE_AUTO 0
 #define QCS_FUSE_SIMT 1   /* FP32 CUDA-core block kernel (k <= 5)          */
-#define QCS_FUSE_TENSOR 2 /* tcgen05 split-BF16x3 block kernel (k <= 6)    */
+#define QCS_FUSE_TENSOR 2 /* tcgen05 split-BF16x3 block kernels (k <= 7)   */
 #define QCS_PARTITION_GREEDY 0
 #define QCS_PARTITION_LEARNED 1
 

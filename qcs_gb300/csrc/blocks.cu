@@ -16,6 +16,7 @@
 // blocks belong on the tensor cores (blocks_tc.cu).
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
@@ -294,7 +295,9 @@ static int apply_item(qcs_cuda_state *s, const qcs_cuda_op *ops, const PlanItem 
 }
 
 static int fusion_cap(const qcs_cuda_state *s, int k, int engine) {
-  int kcap = (engine != QCS_FUSE_SIMT && tc_supported(s, 6)) ? 6 : kSimtMaxK;
+  int kcap = kSimtMaxK;
+  if (engine != QCS_FUSE_SIMT && tc_supported(s, 7)) kcap = 7;
+  else if (engine != QCS_FUSE_SIMT && tc_supported(s, 6)) kcap = 6;
   if (k > kcap) k = kcap;
   if (k > s->n) k = s->n;
   return k;
@@ -456,8 +459,10 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
     return execute_plan(s, ops, s->plans->plan, engine, s->plans, nullptr);
   std::vector<PlanItem> plan;
   if (learned) {
+    // the cost model is trained on blocks of at most 6 qubits
     const bool simt_only = engine == QCS_FUSE_SIMT;
-    plan = partition_learned(ops, count, s->n, k, s->cm, !simt_only && tc_supported(s, 5),
+    plan = partition_learned(ops, count, s->n, std::min(k, 6), s->cm,
+                             !simt_only && tc_supported(s, 5),
                              !simt_only && tc_supported(s, 6), nullptr, nullptr, nullptr);
   } else {
     PartitionOptions po;
@@ -494,7 +499,7 @@ int collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, int km
                     float *feats, float *ms, int max, int *written) {
   int rc = validate_ops(s, ops, count);
   if (rc) return rc;
-  kmax = fusion_cap(s, kmax < 1 ? 1 : kmax, engine);
+  kmax = std::min(fusion_cap(s, kmax < 1 ? 1 : kmax, engine), 6);  // the model's categories
   PartitionOptions po;
   po.kmax = kmax;
   po.cost = nullptr;

@@ -46,6 +46,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -102,8 +103,47 @@ struct TcShape {
   static_assert(TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation size");
 };
 
-// An upload slot: the k = 6 image, then the block's 64 row sums (float2).
-constexpr size_t kImgSlotBytes = TcShape<64>::IMG_BYTES + 64 * 8;
+// k = 7 (KA = 128): the complex form.  The real form of the matrix would be
+// 256 x 256 reals, 256 KB of shared memory in hi + lo, so this kernel keeps
+// the real and imaginary parts apart:
+//   Re Y = Xr Ur^T - Xi Ui^T,   Im Y = Xr Ui^T + Xi Ur^T,
+// A = the tile's real or imaginary parts (M = 128 columns x K = 128
+// amplitudes), B = Re U or Im U (N = 128 outputs x K = 128 inputs), the
+// minus sign from the instruction descriptor's negate-B bit.  The matrix
+// takes 4 x 32 KB (Ur, Ui; hi, lo).  A tile (16384 amplitudes) reaches the
+// tensor cores as four K-chunks of 32 amplitudes, each 4 x 8 KB (Xr, Xi;
+// hi, lo) in 64-byte swizzle atoms, through two shared-memory stages, so
+// that the producers convert one chunk while the tensor cores multiply the
+// other.  (One stage of 64-amplitude chunks, the 128-byte layout of the
+// other kernel, serialised conversion and MMAs: 0.58-0.63 of HBM at 30
+// qubits.)  The accumulators (Re, Im) take 256 TMEM columns per tile,
+// double buffered.
+struct Tc7 {
+  static constexpr int KA = 128;                   // amplitudes per column
+  static constexpr int KC = 32;                    // amplitudes per K-chunk
+  static constexpr int CHUNKS = KA / KC;           // per tile
+  static constexpr int N = KA;                     // UMMA N: outputs of one part
+  static constexpr int CH_BYTES = kTcM * KC * 2;   // one bf16 chunk operand
+  static constexpr int U_BYTES = N * KA * 2;       // one bf16 matrix operand
+  static constexpr int UPT = kTcM * KC / 8 / kTcProdThreads;  // 8-amplitude units per producer
+  static constexpr int TMEM_COLS = 512;            // [stage][re, im][N]
+  static constexpr int OFF_A = 0;                  // [stage][re hi, re lo, im hi, im lo][CH_BYTES]
+  static constexpr int OFF_B = 8 * CH_BYTES;       // [re hi, re lo, im hi, im lo][U_BYTES]
+  static constexpr int OFF_COL = OFF_B + 4 * U_BYTES;
+  static constexpr int OFF_BLK = OFF_COL + kTcM * 8;
+  static constexpr int OFF_SQ = OFF_BLK + KA * 8;  // float [slot 4][half][column]
+  static constexpr int OFF_BETA = OFF_SQ + kSqSlots * 2 * kTcM * 4;  // float2[KA]
+  static constexpr int OFF_EPI = OFF_BETA + KA * 8;  // kLowMode staging
+  static constexpr int OFF_BAR = OFF_EPI + kTcEpiWarps * 32 * kEpiPitch * 4;
+  static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
+  static constexpr int SMEM = OFF_MISC + 16 + 1024;
+  static constexpr int IMG_BYTES = 4 * U_BYTES;
+  static_assert(SMEM <= 232448, "exceeds the 227 KB shared-memory opt-in");
+  static_assert(UPT == 2 && CHUNKS % 2 == 0, "producer shares and stage pairs");
+};
+
+// An upload slot: the largest (k = 7) image, then the block's row sums (float2).
+constexpr size_t kImgSlotBytes = Tc7::IMG_BYTES + Tc7::KA * 8;
 
 struct TcGeom {
   i64 n_tiles;
@@ -113,7 +153,7 @@ struct TcGeom {
   int pf_ahead;       // tiles ahead whose pieces are prefetched
   signed char freeq[40];
   i64 col_off[kTcM];  // column m -> offset (bits of m on the column qubits)
-  i64 blk_off[64];    // block index a -> offset (bit j of a on qubits[j])
+  i64 blk_off[128];   // block index a -> offset (bit j of a on qubits[j])
   i64 run_off[128];   // piece j -> offset of its first amplitude
 };
 
@@ -123,7 +163,9 @@ struct TcGeom {
 // 0.885, 3 tiles ahead 0.85-0.92 depending on the piece.  Whole runs are
 // kept: on the 30-qubit brick benchmark pieces of 2^9 measured 1.5 % slower,
 // and k = 5 blocks 14 % slower.
-static int pf_ahead() { return 2; }
+// k = 7 tiles are twice as large: 2 tiles ahead measured 0.65 of HBM on
+// four placements at 28 qubits (mean), 1 tile ahead 0.79, none 0.71.
+static int pf_ahead(int k) { return k == 7 ? 1 : 2; }
 static int pf_piece_bits() { return 16; }
 
 __device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
@@ -545,6 +587,411 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
+// k = 7 (the complex form, Tc7).  Same roles, waits and fused epilogue as
+// k_block_tc; what differs is the operand layout and the chunked pipeline:
+//   producers  convert chunk q (tile q / 4, amplitudes 32 (q % 4) ..) into
+//              stage q % 2 once the MMAs of chunk q - 2 are done, holding
+//              chunks q + 1 and q + 2 in flight in registers meanwhile;
+//   MMA        12 products per 16-amplitude K-step (Re, Im x 3 split terms x
+//              2 parts), committing a stage back after every chunk and the
+//              accumulator pair after a tile's last chunk;
+//   epilogue   reads Re and Im of 32 outputs at a time (two tcgen05.ld).
+// In kLowMode (the block is qubits 0..6) a column is 128 adjacent
+// amplitudes: a producer warp instruction reads 256 contiguous bytes of each
+// of 2 columns, and the epilogue transposes 32 x 16 results through shared
+// memory, as in k_block_tc.
+template <int MODE, bool FUSED>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_block_tc7(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
+                const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err) {
+  using S = Tc7;
+  extern __shared__ uint8_t smem_dyn[];
+  const uint32_t raw = smem_u32(smem_dyn);
+  uint8_t *smem = smem_dyn + ((1024u - (raw & 1023u)) & 1023u);
+  uint8_t *sA = smem + S::OFF_A;
+  uint8_t *sB = smem + S::OFF_B;
+  i64 *col_off = reinterpret_cast<i64 *>(smem + S::OFF_COL);
+  i64 *blk_off = reinterpret_cast<i64 *>(smem + S::OFF_BLK);
+  float *colsq = reinterpret_cast<float *>(smem + S::OFF_SQ);
+  float *epi = reinterpret_cast<float *>(smem + S::OFF_EPI);
+  const uint32_t bar0 = smem_u32(smem + S::OFF_BAR);  // 8-byte barriers:
+  // 0,1 chunk_full[stage]  2,3 chunk_free[stage]  4,5 acc_full[acc]
+  // 6,7 acc_empty[acc]  8 drain  9..12 sq_full[slot]: a tile's column norms
+  auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::OFF_MISC);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::OFF_MISC + 4);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    mbar_init(bar(0), kTcProdThreads);
+    mbar_init(bar(1), kTcProdThreads);
+    mbar_init(bar(2), 1);
+    mbar_init(bar(3), 1);
+    mbar_init(bar(4), 1);
+    mbar_init(bar(5), 1);
+    mbar_init(bar(6), kTcEpiThreads);
+    mbar_init(bar(7), kTcEpiThreads);
+    mbar_init(bar(8), 1);
+    for (int k = 0; k < kSqSlots; k++) mbar_init(bar(9 + k), kTcProdThreads);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  for (int i = tid; i < kTcM; i += kTcThreads) col_off[i] = g.col_off[i];
+  for (int i = tid; i < S::KA; i += kTcThreads) blk_off[i] = g.blk_off[i];
+  {
+    uint4 *dst = reinterpret_cast<uint4 *>(sB);
+    for (int i = tid; i < S::IMG_BYTES / 16; i += kTcThreads) dst[i] = bimg[i];
+  }
+  float2 *beta = reinterpret_cast<float2 *>(smem + S::OFF_BETA);
+  if (FUSED && diffuse_sum) {  // as in k_block_tc: beta[a] = 2m * (row sum a of U)
+    const float tr = (float)(2.0 * (diffuse_sum[0] * inv_n));
+    const float ti = (float)(2.0 * (diffuse_sum[1] * inv_n));
+    const float2 *rows = reinterpret_cast<const float2 *>(bimg + S::IMG_BYTES / 16);
+    for (int i = tid; i < S::KA; i += kTcThreads) {
+      const float2 r = rows[i];
+      beta[i] = make_float2(tr * r.x - ti * r.y, tr * r.y + ti * r.x);
+    }
+  }
+  fence_async_shared();
+  if (warp == kTcMmaWarp) {
+    tmem_alloc(smem_u32(tmem_slot), S::TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp >= kTcEpiWarps && warp < kTcMmaWarp) {
+    // ---------------- producers ----------------
+    // Thread p keeps column mc = p % 128; of a chunk's 4 units of 8
+    // amplitudes it takes units p / 128 and p / 128 + 2.  Chunk q's
+    // amplitudes are loaded into register set q % 2 while chunk q - 2 is
+    // converted out of it, two chunks ahead of their conversion.  Column-norm
+    // slot it % 4 is free when tile it's last chunk is converted: the MMAs of
+    // its earlier chunks ran, so the epilogue of tile it - 2 (and with it
+    // that of tile it - 4, the slot's last reader) is done.
+    const int p = tid - kTcEpiThreads;
+    const int mc = p & (kTcM - 1);
+    const int pw = p >> 5;
+    constexpr int LSTEPS = kTcM / (2 * kTcProdWarps);  // kLowMode: 2-column steps per chunk
+    float2 xc[2][S::UPT][8];   // other modes: [chunk parity][unit][amplitude]
+    float4 xl[2][LSTEPS];      // kLowMode: [chunk parity][step]
+    float partl[LSTEPS];       // kLowMode: per-step column norms over a tile
+    const TileWalk w = tile_walk(g);
+    const i64 nq = (i64)S::CHUNKS * w.count;  // chunks, an even number
+    auto load_chunk = [&](auto bc, i64 q) {
+      constexpr int b = decltype(bc)::value;
+      const i64 base = tile_base(w.at(q / S::CHUNKS), g);
+      const int c = (int)(q % S::CHUNKS);
+      if constexpr (MODE == kLowMode) {
+#pragma unroll
+        for (int i = 0; i < LSTEPS; i++) {
+          const int m = pw * 2 * LSTEPS + 2 * i + (lane >> 4);
+          xl[b][i] = *reinterpret_cast<const float4 *>(v + base + col_off[m] + c * S::KC +
+                                                       2 * (lane & 15));
+        }
+      } else {
+        const float2 *src = v + base + col_off[mc];
+#pragma unroll
+        for (int i = 0; i < S::UPT; i++) {
+          const int a = c * S::KC + 8 * ((p >> 7) + 2 * i);
+          if constexpr (MODE == kPairMode) {
+#pragma unroll
+            for (int e = 0; e < 8; e += 2) {
+              const float4 t = *reinterpret_cast<const float4 *>(src + blk_off[a + e]);
+              xc[b][i][e] = make_float2(t.x, t.y);
+              xc[b][i][e + 1] = make_float2(t.z, t.w);
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < 8; e++) xc[b][i][e] = src[blk_off[a + e]];
+          }
+        }
+      }
+    };
+    float part = 0.f;
+    // hi and lo of two amplitudes' real and imaginary parts
+    auto split2 = [&](float2 x0, float2 x1, uint32_t *wd) {
+      const __nv_bfloat162 rh = __floats2bfloat162_rn(x0.x, x1.x);
+      const __nv_bfloat162 ih = __floats2bfloat162_rn(x0.y, x1.y);
+      const float2 rf = __bfloat1622float2(rh), imf = __bfloat1622float2(ih);
+      const __nv_bfloat162 rl = __floats2bfloat162_rn(x0.x - rf.x, x1.x - rf.y);
+      const __nv_bfloat162 il = __floats2bfloat162_rn(x0.y - imf.x, x1.y - imf.y);
+      wd[0] = *reinterpret_cast<const uint32_t *>(&rh);
+      wd[1] = *reinterpret_cast<const uint32_t *>(&rl);
+      wd[2] = *reinterpret_cast<const uint32_t *>(&ih);
+      wd[3] = *reinterpret_cast<const uint32_t *>(&il);
+      return x0.x * x0.x + x0.y * x0.y + x1.x * x1.x + x1.y * x1.y;
+    };
+    auto convert_chunk = [&](auto bc) {
+      constexpr int b = decltype(bc)::value;
+      uint8_t *st = sA + b * 4 * S::CH_BYTES;
+      if constexpr (MODE == kLowMode) {
+#pragma unroll
+        for (int i = 0; i < LSTEPS; i++) {
+          const float4 x = xl[b][i];
+          const int m = pw * 2 * LSTEPS + 2 * i + (lane >> 4);
+          uint32_t wd[4];
+          partl[i] += split2(make_float2(x.x, x.y), make_float2(x.z, x.w), wd);
+          const int off = sw64_offset(m, 2 * (lane & 15));
+#pragma unroll
+          for (int o = 0; o < 4; o++) *reinterpret_cast<uint32_t *>(st + o * S::CH_BYTES + off) = wd[o];
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < S::UPT; i++) {
+          const int j = (p >> 7) + 2 * i;
+          uint32_t wd[4][4];  // [re hi, re lo, im hi, im lo][pair of amplitudes]
+#pragma unroll
+          for (int e = 0; e < 8; e += 2) {
+            uint32_t t[4];
+            part += split2(xc[b][i][e], xc[b][i][e + 1], t);
+#pragma unroll
+            for (int o = 0; o < 4; o++) wd[o][e / 2] = t[o];
+          }
+          const int off = sw64_offset(mc, 8 * j);
+#pragma unroll
+          for (int o = 0; o < 4; o++)
+            *reinterpret_cast<uint4 *>(st + o * S::CH_BYTES + off) =
+                make_uint4(wd[o][0], wd[o][1], wd[o][2], wd[o][3]);
+        }
+      }
+    };
+    // the tile's column norms into slot it % 4: kLowMode sums each column's
+    // 16 lanes (fixed order); otherwise threads p and p + 128 hold the halves
+    auto store_norms = [&](i64 it) {
+      float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
+      if constexpr (MODE == kLowMode) {
+#pragma unroll
+        for (int i = 0; i < LSTEPS; i++) {
+          float x = partl[i];
+#pragma unroll
+          for (int o = 1; o < 16; o <<= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+          if ((lane & 15) == 0) {
+            const int m = pw * 2 * LSTEPS + 2 * i + (lane >> 4);
+            sq[m] = x;
+            sq[kTcM + m] = 0.f;
+          }
+        }
+      } else {
+        sq[(p >> 7) * kTcM + mc] = part;
+      }
+    };
+    // one chunk: false when the CTA is aborting
+    auto step = [&](auto bc, i64 q) -> bool {
+      constexpr int b = decltype(bc)::value;
+      const i64 it = q / S::CHUNKS;
+      const int c = (int)(q % S::CHUNKS);
+      if (c == 0 && p < g.nruns && it + g.pf_ahead < w.count)
+        prefetch_l2(v + tile_base(w.at(it + g.pf_ahead), g) + g.run_off[p],
+                    (uint32_t)g.run_bytes);
+      // stage b is free once the MMAs of chunk q - 2 are done
+      if (q >= 2 && !wait_bar(bar(2 + b), (uint32_t)(((q - 2) >> 1) & 1), abort_flag, err, 1))
+        return false;
+      if (c == 0) {
+        part = 0.f;
+#pragma unroll
+        for (int i = 0; i < LSTEPS; i++) partl[i] = 0.f;
+      }
+      convert_chunk(bc);
+      if (q + 2 < nq) load_chunk(bc, q + 2);
+      if (c == S::CHUNKS - 1) store_norms(it);
+      fence_async_shared();
+      mbar_arrive(bar(b));
+      if (c == S::CHUNKS - 1) mbar_arrive(bar(9 + (int)(it % kSqSlots)));
+      return true;
+    };
+    const std::integral_constant<int, 0> b0{};
+    const std::integral_constant<int, 1> b1{};
+    if (nq > 0) {
+      load_chunk(b0, 0);
+      load_chunk(b1, 1);
+    }
+    for (i64 q = 0; q < nq; q += 2)
+      if (!step(b0, q) || !step(b1, q + 1)) break;
+  } else if (warp == kTcMmaWarp) {
+    // ---------------- MMA issue ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(kTcM, S::N);
+      constexpr uint32_t idesc_neg = idesc | (1u << 14);  // negate B
+      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+      const TileWalk w = tile_walk(g);
+      bool ok = true;
+      for (i64 it = 0; ok && it < w.count; ++it) {
+        const int acc_st = (int)(it & 1);
+        if (it >= 2 &&
+            !wait_bar(bar(6 + acc_st), (uint32_t)(((it - 2) >> 1) & 1), abort_flag, err, 3))
+          break;
+        const uint32_t dr = tmem + (uint32_t)(acc_st * 2 * S::N), di = dr + (uint32_t)S::N;
+        for (int c = 0; c < S::CHUNKS; c++) {
+          const i64 q = it * S::CHUNKS + c;
+          const int b = (int)(q & 1);
+          if (!wait_bar(bar(b), (uint32_t)((q >> 1) & 1), abort_flag, err, 2)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t as = a0 + (uint32_t)(b * 4 * S::CH_BYTES);
+#pragma unroll
+          for (int s = 0; s < S::KC / 16; s++) {
+            const int kk = c * S::KC + 16 * s;  // K index into the matrix
+            const uint32_t ka = (uint32_t)(s * 32);
+            const uint32_t kb = (uint32_t)((kk >> 6) * (S::N * 128) + (kk & 63) * 2);
+            const uint64_t xrh = sw64_desc(as + 0 * S::CH_BYTES + ka);
+            const uint64_t xrl = sw64_desc(as + 1 * S::CH_BYTES + ka);
+            const uint64_t xih = sw64_desc(as + 2 * S::CH_BYTES + ka);
+            const uint64_t xil = sw64_desc(as + 3 * S::CH_BYTES + ka);
+            const uint64_t urh = sw128_desc(b0 + 0 * S::U_BYTES + kb);
+            const uint64_t url = sw128_desc(b0 + 1 * S::U_BYTES + kb);
+            const uint64_t uih = sw128_desc(b0 + 2 * S::U_BYTES + kb);
+            const uint64_t uil = sw128_desc(b0 + 3 * S::U_BYTES + kb);
+            const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
+            umma_bf16(dr, xrh, urh, idesc, acc);  // Re += Xr Ur
+            umma_bf16(dr, xrh, url, idesc, 1u);
+            umma_bf16(dr, xrl, urh, idesc, 1u);
+            umma_bf16(dr, xih, uih, idesc_neg, 1u);  // Re -= Xi Ui
+            umma_bf16(dr, xih, uil, idesc_neg, 1u);
+            umma_bf16(dr, xil, uih, idesc_neg, 1u);
+            umma_bf16(di, xrh, uih, idesc, acc);  // Im += Xr Ui
+            umma_bf16(di, xrh, uil, idesc, 1u);
+            umma_bf16(di, xrl, uih, idesc, 1u);
+            umma_bf16(di, xih, urh, idesc, 1u);  // Im += Xi Ur
+            umma_bf16(di, xih, url, idesc, 1u);
+            umma_bf16(di, xil, urh, idesc, 1u);
+          }
+          umma_commit(bar(2 + b));
+        }
+        if (ok) umma_commit(bar(4 + acc_st));
+      }
+      umma_commit(bar(8));
+      long long t0 = clock64();
+      while (!mbar_try_wait(bar(8), 0)) {
+        if (clock64() - t0 > kWaitCycles) {
+          atomicExch(err, 4);
+          break;
+        }
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- epilogue ----------------
+    const int m = tid;  // TMEM lane = tile column
+    const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
+    const TileWalk w = tile_walk(g);
+    double sum_re = 0.0, sum_im = 0.0;
+    for (i64 it = 0; it < w.count; ++it) {
+      const i64 tile = w.at(it);
+      const int acc_st = (int)(it & 1);
+      if (!wait_bar(bar(4 + acc_st), (uint32_t)((it >> 1) & 1), abort_flag, err, 5)) break;
+      if (!wait_bar(bar(9 + (int)(it % kSqSlots)), (uint32_t)((it / kSqSlots) & 1), abort_flag,
+                    err, 6))
+        break;
+      tc_fence_after();
+      const uint32_t tr = tmem + lane_addr + (uint32_t)(acc_st * 2 * S::N);
+      const uint32_t ti = tr + (uint32_t)S::N;
+      float scale = 1.f;
+      if (renorm) {
+        float out = 0.f;
+#pragma unroll 1
+        for (int cc = 0; cc < 2 * S::N / 64; cc++) {  // Re then Im: adjacent columns
+          float acc[64];
+          tmem_ld64(tr + 64 * cc, acc);
+#pragma unroll
+          for (int q = 0; q < 64; q++) out += acc[q] * acc[q];
+        }
+        const float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
+        const float in = sq[m] + sq[kTcM + m];
+        if (out > 0.f) scale = sqrtf(in / out);
+      }
+      const i64 tbase = tile_base(tile, g);
+      float2 *dst = v + tbase + col_off[m];
+#pragma unroll 1
+      for (int gq = 0; gq < S::N / 32; gq++) {
+        float re[32], im[32];
+        tmem_ld32(tr + 32 * gq, re);
+        tmem_ld32(ti + 32 * gq, im);
+        float pr = 0.f, pi = 0.f;
+#pragma unroll
+        for (int q = 0; q < 32; q++) {
+          re[q] *= scale;
+          im[q] *= scale;
+          if constexpr (FUSED) {
+            if (diffuse_sum) {
+              const float2 b = beta[32 * gq + q];
+              re[q] = b.x - re[q];
+              im[q] = b.y - im[q];
+            }
+            pr += re[q];
+            pi += im[q];
+          }
+        }
+        if constexpr (FUSED) {
+          if (sum_out) {
+            sum_re += (double)pr;
+            sum_im += (double)pi;
+          }
+        }
+        if constexpr (MODE == kLowMode) {
+          // 32 columns x 16 outputs at a time through the warp's staging rows;
+          // then lanes 0-15 store column j and lanes 16-31 column j + 1, one
+          // amplitude each: two full 128-byte lines per instruction
+          float *buf = epi + warp * 32 * kEpiPitch;
+          const int half = lane >> 4, row = lane & 15;
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+#pragma unroll
+            for (int q = 0; q < 16; q++)
+              *reinterpret_cast<float2 *>(buf + lane * kEpiPitch + 2 * q) =
+                  make_float2(re[16 * h + q], im[16 * h + q]);
+            __syncwarp();
+#pragma unroll 4
+            for (int j = 0; j < 32; j += 2) {
+              const float2 val =
+                  *reinterpret_cast<const float2 *>(buf + (j + half) * kEpiPitch + 2 * row);
+              v[tbase + col_off[warp * 32 + j + half] + 32 * gq + 16 * h + row] = val;
+            }
+            __syncwarp();
+          }
+        } else if constexpr (MODE == kPairMode) {
+#pragma unroll
+          for (int q = 0; q < 32; q += 2)
+            *reinterpret_cast<float4 *>(dst + blk_off[32 * gq + q]) =
+                make_float4(re[q], im[q], re[q + 1], im[q + 1]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 32; q++) dst[blk_off[32 * gq + q]] = make_float2(re[q], im[q]);
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(bar(6 + acc_st));
+    }
+    if (FUSED && sum_out) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sum_re += __shfl_xor_sync(0xffffffffu, sum_re, o);
+        sum_im += __shfl_xor_sync(0xffffffffu, sum_im, o);
+      }
+      if (lane == 0) {
+        ReduceSlot r;
+        r.a = sum_re;
+        r.b = sum_im;
+        r.c = 0.0;
+        r.d = 0.0;
+        sum_out[blockIdx.x * kTcEpiWarps + warp] = r;
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kTcMmaWarp) {
+    tc_fence_after();
+    tmem_dealloc(tmem, S::TMEM_COLS);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -583,7 +1030,7 @@ void tc_release(TcRing *r) {
 }
 
 bool tc_supported(const qcs_cuda_state *s, int k) {
-  return s->prec == QCS_CUDA_C64 && s->sem == QCS_CUDA_PHYSICAL && (k == 5 || k == 6) &&
+  return s->prec == QCS_CUDA_C64 && s->sem == QCS_CUDA_PHYSICAL && k >= 5 && k <= 7 &&
          s->n >= k + 7 && s->n - k - 7 <= 40 && s->dev.cc_major == 10 && s->dev.cc_minor == 3;
 }
 
@@ -612,6 +1059,32 @@ static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int r
     k_block_tc<KA, MODE, false><<<grid, kTcThreads, S::SMEM, s->stream>>>(
         (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err);
   return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
+}
+
+template <int MODE>
+static int launch_tc7(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int renorm,
+                      const double *diffuse_sum, ReduceSlot *sum_out) {
+  static bool configured = false;
+  if (!configured) {
+    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc7<MODE, false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Tc7::SMEM),
+                        "cudaFuncSetAttribute(tcgen05 block, k = 7)");
+    if (!rc)
+      rc = check_cuda(cudaFuncSetAttribute(k_block_tc7<MODE, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, Tc7::SMEM),
+                      "cudaFuncSetAttribute(tcgen05 block, k = 7, fused)");
+    if (rc) return rc;
+    configured = true;
+  }
+  const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
+  prof_begin(s);
+  if (diffuse_sum || sum_out)
+    k_block_tc7<MODE, true><<<grid, kTcThreads, Tc7::SMEM, s->stream>>>(
+        (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err);
+  else
+    k_block_tc7<MODE, false><<<grid, kTcThreads, Tc7::SMEM, s->stream>>>(
+        (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err);
+  return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05, k = 7)");
 }
 
 // Whether U is unitary (to FP64 rounding): unitary blocks get the
@@ -749,17 +1222,20 @@ static void tc_prepare(const qcs_cuda_state *s, int k, const int *qubits_in, con
         if ((run >> (b - R)) & 1) o |= 1LL << tq[b];
       g.run_off[j] = o;
     }
-    g.pf_ahead = pf_ahead();
+    g.pf_ahead = pf_ahead(k);
   }
   bool low = true;  // the block is exactly qubits 0..k-1
   for (int j = 0; j < k; j++) low = low && qubits[j] == j;
   out.k = k;
   out.mode = low ? kLowMode : (qubits[0] == 0 ? kPairMode : kColMode);
   out.renorm = (known_unitary || is_unitary(u, KA)) ? 1 : 0;
-  const size_t img = k == 6 ? TcShape<64>::IMG_BYTES : TcShape<32>::IMG_BYTES;
+  const size_t img = k == 7   ? Tc7::IMG_BYTES
+                     : k == 6 ? TcShape<64>::IMG_BYTES
+                              : TcShape<32>::IMG_BYTES;
   out.image_bytes = img + (size_t)KA * 8;
   out.image.assign(out.image_bytes, 0);
-  if (k == 6) make_image<64>(u, out.image.data());
+  if (k == 7) make_image7(u, out.image.data());
+  else if (k == 6) make_image<64>(u, out.image.data());
   else make_image<32>(u, out.image.data());
   float *rows = reinterpret_cast<float *>(out.image.data() + img);
   for (int a = 0; a < KA; a++) {
@@ -786,7 +1262,11 @@ static int tc_launch(qcs_cuda_state *s, const TcResident &b, const uint4 *img,
   const double *dsum = diffuse_in ? s->d_result + 4 : nullptr;
   ReduceSlot *sout = sum_out ? s->d_partials : nullptr;
   const TcGeom &g = b.g;
-  if (b.k == 6)
+  if (b.k == 7)
+    rc = b.mode == kLowMode    ? launch_tc7<kLowMode>(s, g, img, b.renorm, dsum, sout)
+         : b.mode == kPairMode ? launch_tc7<kPairMode>(s, g, img, b.renorm, dsum, sout)
+                               : launch_tc7<kColMode>(s, g, img, b.renorm, dsum, sout);
+  else if (b.k == 6)
     rc = b.mode == kLowMode    ? launch_tc<64, kLowMode>(s, g, img, b.renorm, dsum, sout)
          : b.mode == kPairMode ? launch_tc<64, kPairMode>(s, g, img, b.renorm, dsum, sout)
                                : launch_tc<64, kColMode>(s, g, img, b.renorm, dsum, sout);

@@ -23,6 +23,13 @@ __host__ __device__ __forceinline__ int sw128_offset(int r, int k, int R) {
   return kb * (R * 128) + (r >> 3) * 1024 + (r & 7) * 128 + ((chunk ^ (r & 7)) << 4) + e * 2;
 }
 
+// The same for 64-byte swizzle atoms (8 rows x 32 elements, 16-byte chunks
+// permuted by XOR with bits 1-2 of the row): an operand whose K extent is 32.
+__host__ __device__ __forceinline__ int sw64_offset(int r, int k) {
+  const int chunk = (k >> 3) & 3, e = k & 7;
+  return (r >> 3) * 512 + (r & 7) * 64 + ((chunk ^ ((r >> 1) & 3)) << 4) + e * 2;
+}
+
 // ---- PTX wrappers ---------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -132,6 +139,17 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
+// The same for the 64-byte swizzle: 8-row groups 512 bytes apart.
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;             // LBO (ignored for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;    // SBO
+  d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
+  d |= (uint64_t)4 << 61;             // SWIZZLE_64B
+  return d;
+}
+
 // Instruction descriptor: kind::f16, A = B = bf16, D = fp32, both K-major.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
@@ -190,6 +208,26 @@ static void make_image(const double *u, uint8_t *img) {
           hi[off] = h;
           lo[off] = l;
         }
+    }
+}
+
+// Block matrix u (128 x 128 complex, row-major) -> the four swizzled
+// operands of the k = 7 kernel: Re U hi, Re U lo, Im U hi, Im U lo, each
+// N = 128 output rows x K = 128 inputs.
+static void make_image7(const double *u, uint8_t *img) {
+  constexpr int KA = 128, U_BYTES = KA * KA * 2;
+  memset(img, 0, 4 * U_BYTES);
+  uint16_t *op[4];
+  for (int o = 0; o < 4; o++) op[o] = reinterpret_cast<uint16_t *>(img + o * U_BYTES);
+  for (int ao = 0; ao < KA; ao++)
+    for (int ai = 0; ai < KA; ai++) {
+      const int off = sw128_offset(ao, ai, KA) / 2;
+      for (int part = 0; part < 2; part++) {
+        const double x = u[2 * (ao * KA + ai) + part];
+        const uint16_t h = bf16_rn((float)x);
+        op[2 * part][off] = h;
+        op[2 * part + 1][off] = bf16_rn((float)(x - (double)bf16_to_float(h)));
+      }
     }
 }
 

@@ -301,11 +301,12 @@ def test_fused_circuit_simt(k):
 TC_ATOL = 5e-5
 
 
-@pytest.mark.parametrize("k", [5, 6])
+@pytest.mark.parametrize("k", [5, 6, 7])
 @pytest.mark.parametrize("placement", ["col", "pair", "low"])
 def test_apply_block_tensor_cores(k, placement):
     """The kernel's three access modes: qubit 0 a column qubit, qubit 0 in the
-    block, the block exactly qubits 0..k-1; qubits in random order."""
+    block, the block exactly qubits 0..k-1; qubits in random order.  At k = 7
+    (the complex-form kernel) a block on qubits 0..6 runs in the paired mode."""
     n = 15
     rng = np.random.default_rng(10 * k + len(placement))
     for trial in range(3):
@@ -332,7 +333,7 @@ def test_apply_block_tensor_cores(k, placement):
             assert infidelity(a, b) < 1e-8
 
 
-@pytest.mark.parametrize("k,n", [(6, 13), (5, 12), (6, 14)])
+@pytest.mark.parametrize("k,n", [(6, 13), (5, 12), (6, 14), (7, 14), (7, 15)])
 def test_tensor_cores_smallest_states(k, n):
     """The smallest states the tensor engine takes (n = k + 7: one tile, one
     CTA) and a few tiles: every pipeline stage runs with fewer tiles than
@@ -393,18 +394,20 @@ def test_tensor_cores_apply_non_unitary_matrices_as_given():
     norm restore is only for unitary blocks."""
     n = 15
     rng = np.random.default_rng(55)
-    u, _ = np.linalg.qr(rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64)))
-    proj = np.diag([1.0 if i % 3 else 0.0 for i in range(64)]).astype(complex)
-    for m in (0.5 * u, proj, u @ proj):
-        init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
-        init /= np.linalg.norm(init)
-        with capi.State(n, capi.C64) as s, O.OracleState(n) as o:
-            s.set_amplitudes(init)
-            o.set_amplitudes(init)
-            s.apply_block([1, 4, 6, 8, 11, 13], m, capi.FUSE_TENSOR)
-            o.apply_block([1, 4, 6, 8, 11, 13], m)
-            a, b = s.amplitudes(), o.amplitudes()
-            assert np.max(np.abs(a - b)) < TC_ATOL
+    for qubits in ([1, 4, 6, 8, 11, 13], [0, 2, 3, 7, 9, 12, 14]):
+        K = 1 << len(qubits)
+        u, _ = np.linalg.qr(rng.normal(size=(K, K)) + 1j * rng.normal(size=(K, K)))
+        proj = np.diag([1.0 if i % 3 else 0.0 for i in range(K)]).astype(complex)
+        for m in (0.5 * u, proj, u @ proj):
+            init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+            init /= np.linalg.norm(init)
+            with capi.State(n, capi.C64) as s, O.OracleState(n) as o:
+                s.set_amplitudes(init)
+                o.set_amplitudes(init)
+                s.apply_block(qubits, m, capi.FUSE_TENSOR)
+                o.apply_block(qubits, m)
+                a, b = s.amplitudes(), o.amplitudes()
+                assert np.max(np.abs(a - b)) < TC_ATOL
 
 
 def test_tensor_cores_preserve_the_norm_over_many_blocks():
@@ -434,7 +437,7 @@ def test_tensor_engine_rejects_unsupported():
         assert e.value.status == capi.EUNSUP
 
 
-@pytest.mark.parametrize("k", [5, 6])
+@pytest.mark.parametrize("k", [5, 6, 7])
 def test_fused_circuit_tensor_cores(k):
     n = 18
     g = W.brick_circuit(n, 10, 4)
@@ -463,7 +466,7 @@ def test_fused_with_grover_barriers():
 
 
 @pytest.mark.parametrize("engine,k", [(capi.FUSE_SIMT, 5), (capi.FUSE_TENSOR, 6),
-                                      (capi.FUSE_AUTO, 4)])
+                                      (capi.FUSE_AUTO, 4), (capi.FUSE_AUTO, 7)])
 def test_kept_plan_replays_identically(engine, k):
     """A second run of the same op list reuses the kept plan and block
     matrices and gives the same amplitudes, bit for bit, as planning afresh;
@@ -496,11 +499,12 @@ def test_kept_plan_replays_identically(engine, k):
         assert not np.array_equal(a, c)
 
 
-def test_grover_rounds_fuse_diffusion_into_tensor_core_blocks():
+@pytest.mark.parametrize("k", [6, 7])
+def test_grover_rounds_fuse_diffusion_into_tensor_core_blocks(k):
     """QFT + rounds of (Hadamard layer, phase flip, diffusion), fused at width
-    6 on a state the tensor cores take: every diffusion but the last runs
-    inside the following block, and the block before each flip leaves the
-    sum the diffusion needs, so no separate reduction or diffusion sweep
+    6 or 7 on a state the tensor cores take: every diffusion but the last
+    runs inside the following block, and the block before each flip leaves
+    the sum the diffusion needs, so no separate reduction or diffusion sweep
     runs; the state still matches the FP64 oracle."""
     n = 16
     w = W.grover_workload(n, 8, iterations=8)
@@ -509,7 +513,7 @@ def test_grover_rounds_fuse_diffusion_into_tensor_core_blocks():
     full.extend(w.rounds)
     with capi.State(n, capi.C64) as s, oracle_state(n, full) as o:
         s.profile(True)
-        s.run(full, fusion_k=6)
+        s.run(full, fusion_k=k)
         prof = s.profile_read()
         s.profile(False)
         a, b = s.amplitudes(), o.amplitudes()
@@ -519,7 +523,7 @@ def test_grover_rounds_fuse_diffusion_into_tensor_core_blocks():
     assert prof["diffuse"][0] == 1        # the last round's, with no block after it
     assert "reduce" not in prof           # sums come from the blocks' epilogues
     with capi.State(n, capi.C64) as s, oracle_state(n, w.search) as o:
-        s.run(w.search, fusion_k=6)
+        s.run(w.search, fusion_k=k)
         assert s.argmax() == o.argmax() == w.marked
         assert infidelity(s.amplitudes(), o.amplitudes()) < 1e-6
 
