@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--depth", type=int, default=40)
     ap.add_argument("--seed", type=int, default=2026)
-    ap.add_argument("--fusion-k", type=int, default=int(os.environ.get("QCS_BENCH_FUSION_K", "6")))
+    ap.add_argument("--fusion-k", type=int, default=int(os.environ.get("QCS_BENCH_FUSION_K", "7")))
     ap.add_argument("--engine", default=os.environ.get("QCS_BENCH_ENGINE", "auto"),
                     choices=["auto", "simt", "tensor"])
     ap.add_argument("--plain-steps", type=int, default=None,
@@ -793,7 +793,8 @@ def run_learned(args, dist):
             row = {"circuit": kind, "seed": seed, "gates": len(g)}
             for label, k, part in (("unfused", 0, capi.PARTITION_GREEDY),
                                    ("greedy6", 6, capi.PARTITION_GREEDY),
-                                   ("learned", 6, capi.PARTITION_LEARNED)):
+                                   ("learned", 6, capi.PARTITION_LEARNED),
+                                   ("greedy7", 7, capi.PARTITION_GREEDY)):
                 s.set_basis(0)
                 s.run(ops, fusion_k=k, partitioner=part)  # warm-up
                 ts = []
@@ -807,6 +808,7 @@ def run_learned(args, dist):
                 if label != "unfused":
                     row[label + "_state"] = s.amplitudes()
             a, b = row.pop("learned_state"), row.pop("greedy6_state")
+            row.pop("greedy7_state")
             row["infidelity_learned_vs_greedy"] = float(
                 1.0 - abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real))
             del a, b

@@ -190,13 +190,14 @@ int qcs_cuda_plan(const qcs_cuda_op *ops, int count, int num_qubits, int kmax,
 #define QCS_KCLASS_PHASE_MASK 2 /* phase on amplitudes with bits set      */
 #define QCS_KCLASS_CTRL1Q 3     /* controlled 2x2 (control=1 half)        */
 #define QCS_KCLASS_BLOCK_SIMT 4 /* fused block, CUDA cores                */
-#define QCS_KCLASS_BLOCK_TC 5   /* fused block, tensor cores              */
+#define QCS_KCLASS_BLOCK_TC 5   /* fused block (k <= 6), tensor cores     */
 #define QCS_KCLASS_REDUCE 6     /* norm / probability / sum reductions    */
 #define QCS_KCLASS_DIFFUSE 7    /* diffusion update (+ fused sum)         */
 #define QCS_KCLASS_COLLAPSE 8   /* measurement collapse, rescale          */
 #define QCS_KCLASS_SAMPLE 9     /* shot sampling                          */
 #define QCS_KCLASS_OTHER 10     /* set-basis, phase flip, finalisers      */
-#define QCS_KCLASS_COUNT 11
+#define QCS_KCLASS_BLOCK_TC7 11 /* fused 7-qubit block, tensor cores      */
+#define QCS_KCLASS_COUNT 12
 /* enable != 0: from now on bracket every kernel with CUDA events on the
  * state's stream and accumulate device time and algorithmic bytes per
  * class (counters are cleared); enable == 0 stops recording. */

@@ -30,7 +30,7 @@ FUSE_AUTO, FUSE_SIMT, FUSE_TENSOR = 0, 1, 2
 PARTITION_GREEDY, PARTITION_LEARNED = 0, 1
 # QCS_KCLASS_* order (include/qcs_cuda.h)
 KCLASS_NAMES = ("dense1q", "diag1q", "phase_mask", "ctrl1q", "block_simt", "block_tc",
-                "reduce", "diffuse", "collapse", "sample", "other")
+                "reduce", "diffuse", "collapse", "sample", "other", "block_tc7")
 
 
 class QcsCudaError(RuntimeError):

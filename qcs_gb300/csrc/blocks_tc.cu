@@ -1084,7 +1084,7 @@ static int launch_tc7(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int 
   else
     k_block_tc7<MODE, false><<<grid, kTcThreads, Tc7::SMEM, s->stream>>>(
         (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err);
-  return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05, k = 7)");
+  return launched(s, KC_BLOCK_TC7, 2.0 * s->size * 8.0, "apply_block (tcgen05, k = 7)");
 }
 
 // Whether U is unitary (to FP64 rounding): unitary blocks get the

@@ -46,6 +46,7 @@ enum KClass {
   KC_COLLAPSE = QCS_KCLASS_COLLAPSE,
   KC_SAMPLE = QCS_KCLASS_SAMPLE,
   KC_OTHER = QCS_KCLASS_OTHER,
+  KC_BLOCK_TC7 = QCS_KCLASS_BLOCK_TC7,
   KC_COUNT = QCS_KCLASS_COUNT
 };
 
