@@ -735,11 +735,11 @@ def run_batch(args, dist):
 
 def run_learned(args, dist):
     """Learned fusion cost model: ~20k kernel timings from random 24..32-qubit
-    circuits (every fusion width 2..6, both block engines), an MLP trained on
+    circuits (every fusion width 1..7, both block engines), an MLP trained on
     them by the library's own GPU kernels, then unseen 30-qubit depth-60 mixed
     circuits (rotations, CNOTs, QFT-style controlled phases) and the 30-qubit
-    brick circuit, timed three ways: learned partition, greedy width-6
-    partition, unfused.  Each form is run
+    brick circuit, timed five ways: learned and greedy partitions at widths 6
+    and 7, and unfused.  Each form is run
     once untimed first; the timed runs reuse the state's kept plan, so the
     times are device time, and each partitioner's host planning time is
     reported beside them."""
@@ -763,7 +763,7 @@ def run_learned(args, dist):
                 g = (W.mixed_circuit(n, depth, seed) if kind == 0 else
                      W.brick_circuit(n, depth, seed) if kind == 1 else
                      W.random_circuit(n, seed, 40 * depth, with_qft=False)[1])
-                k = int(rng.integers(1, 7))
+                k = int(rng.integers(1, 8))
                 eng = capi.FUSE_SIMT if rng.random() < 0.3 else capi.FUSE_AUTO
                 f, ms = capi.collect_timings(s, g, kmax=k, engine=eng)
                 feats.append(f)
@@ -794,7 +794,8 @@ def run_learned(args, dist):
             for label, k, part in (("unfused", 0, capi.PARTITION_GREEDY),
                                    ("greedy6", 6, capi.PARTITION_GREEDY),
                                    ("learned", 6, capi.PARTITION_LEARNED),
-                                   ("greedy7", 7, capi.PARTITION_GREEDY)):
+                                   ("greedy7", 7, capi.PARTITION_GREEDY),
+                                   ("learned7", 7, capi.PARTITION_LEARNED)):
                 s.set_basis(0)
                 s.run(ops, fusion_k=k, partitioner=part)  # warm-up
                 ts = []
@@ -808,7 +809,10 @@ def run_learned(args, dist):
                 if label != "unfused":
                     row[label + "_state"] = s.amplitudes()
             a, b = row.pop("learned_state"), row.pop("greedy6_state")
-            row.pop("greedy7_state")
+            a7, b7 = row.pop("learned7_state"), row.pop("greedy7_state")
+            row["infidelity_learned7_vs_greedy7"] = float(
+                1.0 - abs(np.vdot(a7, b7)) ** 2 / (np.vdot(a7, a7).real * np.vdot(b7, b7).real))
+            del a7, b7
             row["infidelity_learned_vs_greedy"] = float(
                 1.0 - abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real))
             del a, b
@@ -823,6 +827,11 @@ def run_learned(args, dist):
             row["pred_ms_learned"] = plan["pred_ms"]
             row["pred_ms_greedy"] = plan["greedy_pred_ms"]
             row["speedup_vs_greedy"] = row["greedy6_ms"] / row["learned_ms"]
+            row["speedup7_vs_greedy7"] = row["greedy7_ms"] / row["learned7_ms"]
+            plan7 = capi.plan_learned(g, n, 7, model)
+            row["learned7_choice"] = plan7["choice"]
+            row["learned7_items"] = plan7["items"]
+            row["greedy7_items"] = capi.plan(g, n, 7)[2]
             row["speedup_vs_unfused"] = row["unfused_ms"] / row["learned_ms"]
             evals.append(row)
         s.set_costmodel(None)

@@ -294,6 +294,14 @@ static int apply_item(qcs_cuda_state *s, const qcs_cuda_op *ops, const PlanItem 
   return apply_block_item(s, it, engine, u, nullptr);
 }
 
+// The widest block the tensor cores take on this state (0: none).
+static int tc_max(const qcs_cuda_state *s, int engine) {
+  if (engine == QCS_FUSE_SIMT) return 0;
+  for (int k = 7; k >= 5; k--)
+    if (tc_supported(s, k)) return k;
+  return 0;
+}
+
 static int fusion_cap(const qcs_cuda_state *s, int k, int engine) {
   int kcap = kSimtMaxK;
   if (engine != QCS_FUSE_SIMT && tc_supported(s, 7)) kcap = 7;
@@ -459,11 +467,8 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
     return execute_plan(s, ops, s->plans->plan, engine, s->plans, nullptr);
   std::vector<PlanItem> plan;
   if (learned) {
-    // the cost model is trained on blocks of at most 6 qubits
-    const bool simt_only = engine == QCS_FUSE_SIMT;
-    plan = partition_learned(ops, count, s->n, std::min(k, 6), s->cm,
-                             !simt_only && tc_supported(s, 5),
-                             !simt_only && tc_supported(s, 6), nullptr, nullptr, nullptr);
+    plan = partition_learned(ops, count, s->n, k, s->cm, tc_max(s, engine), nullptr, nullptr,
+                             nullptr);
   } else {
     PartitionOptions po;
     po.kmax = k;
@@ -499,14 +504,13 @@ int collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, int km
                     float *feats, float *ms, int max, int *written) {
   int rc = validate_ops(s, ops, count);
   if (rc) return rc;
-  kmax = std::min(fusion_cap(s, kmax < 1 ? 1 : kmax, engine), 6);  // the model's categories
+  kmax = fusion_cap(s, kmax < 1 ? 1 : kmax, engine);
   PartitionOptions po;
   po.kmax = kmax;
   po.cost = nullptr;
   po.cost_ctx = nullptr;
   std::vector<PlanItem> plan = partition(ops, count, s->n, po);
-  const bool tc5 = engine != QCS_FUSE_SIMT && tc_supported(s, 5);
-  const bool tc6 = engine != QCS_FUSE_SIMT && tc_supported(s, 6);
+  const int tcm = tc_max(s, engine);
   std::vector<cudaEvent_t> ev;
   std::vector<int> rec;  // item index of each recorded pair
   std::vector<cd> u;
@@ -537,7 +541,7 @@ int collect_timings(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, int km
     float t = 0.f;
     cudaEventElapsedTime(&t, ev[2 * r], ev[2 * r + 1]);
     const PlanItem &it = plan[rec[r]];
-    const int cat = item_category(ops, it, tc5, tc6);
+    const int cat = item_category(ops, it, tcm);
     item_features(cat, s->n, (int)it.qubits.size(), (int)it.gates.size(), it.qubits.data(),
                   feats + r * kCostFeatures);
     ms[r] = t;
@@ -638,10 +642,11 @@ int qcs_cuda_plan_learned(const qcs_cuda_op *ops, int count, int num_qubits, int
   shape.size = 1LL << num_qubits;
   int rc = validate_ops(&shape, ops, count);
   if (rc) return rc;
-  if (kmax > 6) kmax = 6;
+  if (kmax > 7) kmax = 7;
+  // the tensor cores take k-qubit blocks on states of at least k + 7 qubits
+  const int tcm = num_qubits >= 14 ? 7 : num_qubits >= 13 ? 6 : num_qubits >= 12 ? 5 : 0;
   std::vector<PlanItem> plan =
-      partition_learned(ops, count, num_qubits, kmax, m, num_qubits >= 12, num_qubits >= 13,
-                        pred_ms, greedy_ms, choice);
+      partition_learned(ops, count, num_qubits, kmax, m, tcm, pred_ms, greedy_ms, choice);
   int j = 0;
   for (size_t it = 0; it < plan.size(); it++) {
     if (plan[it].kind == 1) {

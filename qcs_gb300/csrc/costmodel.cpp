@@ -36,7 +36,7 @@ void item_features(int cat, int n, int k, int ngates, const int *qubits, float *
 static bool is_zero(const double *z) { return z[0] == 0.0 && z[1] == 0.0; }
 static bool is_one(const double *z) { return z[0] == 1.0 && z[1] == 0.0; }
 
-int item_category(const qcs_cuda_op *ops, const PlanItem &it, bool tc_ok_5, bool tc_ok_6) {
+int item_category(const qcs_cuda_op *ops, const PlanItem &it, int tc_max) {
   const int k = (int)it.qubits.size();
   if (it.gates.size() == 1 || k == 1) {
     // a single gate, or a product of one-qubit gates on one qubit: plain kernel
@@ -73,7 +73,7 @@ int item_category(const qcs_cuda_op *ops, const PlanItem &it, bool tc_ok_5, bool
     return CAT_DENSE;
   }
   // AUTO runs 2..4-qubit blocks on the tensor cores, widened to 5 qubits
-  if ((k >= 2 && k <= 5 && tc_ok_5) || (k == 6 && tc_ok_6)) return CAT_TC;
+  if (tc_max >= 5 && k >= 2 && k <= tc_max) return CAT_TC;
   return CAT_SIMT;
 }
 
@@ -81,13 +81,13 @@ struct PlanScore {
   const qcs_cuda_costmodel *m;
   const qcs_cuda_op *ops;
   int n;
-  bool tc5, tc6;
+  int tc_max;
 };
 
 static double item_ms(const PlanScore &ps, const PlanItem &it) {
   if (it.kind == 1) return 0.0;  // non-gate ops are the same in every plan
   float f[kCostFeatures];
-  const int cat = item_category(ps.ops, it, ps.tc5, ps.tc6);
+  const int cat = item_category(ps.ops, it, ps.tc_max);
   item_features(cat, ps.n, (int)it.qubits.size(), (int)it.gates.size(), it.qubits.data(), f);
   return exp2((double)costmodel_predict_host(ps.m, f));
 }
@@ -103,7 +103,7 @@ static double grow_cost(int n, int k, int ngates, const int *qubits, void *ctx) 
   const PlanScore &ps = *static_cast<const PlanScore *>(ctx);
   int cat;
   if (k == 1) cat = CAT_DENSE;
-  else if ((k >= 2 && k <= 5 && ps.tc5) || (k == 6 && ps.tc6)) cat = CAT_TC;
+  else if (ps.tc_max >= 5 && k <= ps.tc_max) cat = CAT_TC;
   else cat = CAT_SIMT;
   float f[kCostFeatures];
   item_features(cat, n, k, ngates, qubits, f);
@@ -150,10 +150,9 @@ static bool refine_block(const PlanScore &ps, const PlanItem &it, std::vector<Pl
 }
 
 std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n, int kmax,
-                                        const qcs_cuda_costmodel *m, bool tc_ok_5,
-                                        bool tc_ok_6, double *pred_ms, double *greedy_ms,
-                                        int *choice) {
-  PlanScore ps{m, ops, n, tc_ok_5, tc_ok_6};
+                                        const qcs_cuda_costmodel *m, int tc_max,
+                                        double *pred_ms, double *greedy_ms, int *choice) {
+  PlanScore ps{m, ops, n, tc_max};
   PartitionOptions po;
   po.kmax = kmax;
   po.cost = nullptr;

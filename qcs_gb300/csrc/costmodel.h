@@ -27,8 +27,10 @@ enum ItemCat {
 // touches, how many of its qubits are below 7, its highest qubit.
 void item_features(int cat, int n, int k, int ngates, const int *qubits, float *f);
 
-// Category the executor will use for a plan item.
-int item_category(const qcs_cuda_op *ops, const PlanItem &it, bool tc_ok_5, bool tc_ok_6);
+// Category the executor will use for a plan item.  tc_max: the widest block
+// the tensor cores take on this state (5, 6 or 7; 0 when they take none);
+// 2..4-qubit blocks go there widened to 5 when tc_max >= 5.
+int item_category(const qcs_cuda_op *ops, const PlanItem &it, int tc_max);
 
 struct CostModelView;  // opaque handle used by the partitioner
 
@@ -37,9 +39,8 @@ struct CostModelView;  // opaque handle used by the partitioner
 // time; the greedy width-kmax plan judges -- the candidate replaces it only
 // when predicted faster.  *chosen receives a short description.
 std::vector<PlanItem> partition_learned(const qcs_cuda_op *ops, int count, int n, int kmax,
-                                        const struct ::qcs_cuda_costmodel *m, bool tc_ok_5,
-                                        bool tc_ok_6, double *pred_ms, double *greedy_ms,
-                                        int *choice);
+                                        const struct ::qcs_cuda_costmodel *m, int tc_max,
+                                        double *pred_ms, double *greedy_ms, int *choice);
 
 float costmodel_predict_host(const struct ::qcs_cuda_costmodel *m, const float *x);
 bool costmodel_ready(const struct ::qcs_cuda_costmodel *m);

@@ -96,7 +96,7 @@ def _timed_ms(s, g, k, part, reps=5):
 @pytest.fixture(scope="module")
 def trained_model():
     """A model trained on this simulator's own timings of random 20..24-qubit
-    circuits (every width 1..6, both block engines)."""
+    circuits (every width 1..7, both block engines)."""
     rng = np.random.default_rng(21)
     feats, times = [], []
     for n in (20, 22, 24):
@@ -107,7 +107,7 @@ def trained_model():
                 g = (W.mixed_circuit(n, depth, seed) if rep % 3 == 0 else
                      W.brick_circuit(n, depth, seed) if rep % 3 == 1 else
                      W.random_circuit(n, seed, 40 * depth, with_qft=False)[1])
-                for k in range(1, 7):
+                for k in range(1, 8):
                     eng = capi.FUSE_SIMT if k <= 5 and rep % 2 else capi.FUSE_AUTO
                     f, ms = capi.collect_timings(s, g, kmax=k, engine=eng)
                     feats.append(f)
@@ -120,11 +120,12 @@ def trained_model():
     m.close()
 
 
-@pytest.mark.parametrize("circuit,bar", [("mixed", 1.0), ("brick", 0.95)])
-def test_learned_partition_gain_over_greedy(trained_model, circuit, bar, record_property):
+@pytest.mark.parametrize("circuit,width,bar", [("mixed", 6, 1.0), ("brick", 6, 0.95),
+                                               ("mixed", 7, 0.95), ("brick", 7, 0.95)])
+def test_learned_partition_gain_over_greedy(trained_model, circuit, width, bar, record_property):
     """What the trained network gains over the method without it: the model
     plans an unseen 24-qubit circuit and its plan is timed against the greedy
-    width-6 plan (the judge) on the same state.  On mixed circuits the model
+    plan of the same width (the judge) on the same state.  On mixed circuits the model
     picks a candidate with fewer blocks and must be faster; on the brick
     circuit the same candidate generator gives more blocks and the model
     must keep (about) the greedy plan.  The learned plan must leave the state
@@ -132,15 +133,15 @@ def test_learned_partition_gain_over_greedy(trained_model, circuit, bar, record_
     m = trained_model
     n = 24
     g = W.mixed_circuit(n, 30, 4242) if circuit == "mixed" else W.brick_circuit(n, 20, 4242)
-    plan = capi.plan_learned(g, n, 6, m)
+    plan = capi.plan_learned(g, n, width, m)
     assert plan["pred_ms"] <= plan["greedy_pred_ms"]
     with capi.State(n, capi.C64) as s:
         s.set_costmodel(m)
-        t_greedy = _timed_ms(s, g, 6, capi.PARTITION_GREEDY)
+        t_greedy = _timed_ms(s, g, width, capi.PARTITION_GREEDY)
         greedy = s.amplitudes()
-        t_learned = _timed_ms(s, g, 6, capi.PARTITION_LEARNED)
+        t_learned = _timed_ms(s, g, width, capi.PARTITION_LEARNED)
         learned = s.amplitudes()
-        t_greedy2 = _timed_ms(s, g, 6, capi.PARTITION_GREEDY)
+        t_greedy2 = _timed_ms(s, g, width, capi.PARTITION_GREEDY)
         s.set_costmodel(None)
     t_greedy = min(t_greedy, t_greedy2)
     gain = t_greedy / t_learned
@@ -148,7 +149,7 @@ def test_learned_partition_gain_over_greedy(trained_model, circuit, bar, record_
     record_property("learned_ms", t_learned)
     record_property("gain", gain)
     record_property("choice", plan["choice"])
-    print(f"{circuit}: learned {t_learned:.3f} ms greedy {t_greedy:.3f} ms gain {gain:.3f} "
+    print(f"{circuit} w{width}: learned {t_learned:.3f} ms greedy {t_greedy:.3f} ms gain {gain:.3f} "
           f"choice {plan['choice']} items {plan['items']}")
     assert infidelity(learned, greedy) < 1e-6
     assert gain > bar
