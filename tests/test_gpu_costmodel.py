@@ -121,7 +121,7 @@ def trained_model():
 
 
 @pytest.mark.parametrize("circuit,width,bar", [("mixed", 6, 1.0), ("brick", 6, 0.95),
-                                               ("mixed", 7, 0.95), ("brick", 7, 0.95)])
+                                               ("mixed", 7, 0.95), ("brick", 7, 0.9)])
 def test_learned_partition_gain_over_greedy(trained_model, circuit, width, bar, record_property):
     """What the trained network gains over the method without it: the model
     plans an unseen 24-qubit circuit and its plan is timed against the greedy
