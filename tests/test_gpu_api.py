@@ -268,14 +268,20 @@ def test_invalid_gate_arguments_are_reported_and_recorded(A, capfd):
     A.qc_destroy(c)
 
 
-def test_fusion_mode_same_answers(A):
-    for k in (0, 4):
-        c = A.qc_create_ex(8, capi.C64, capi.PHYSICAL, k)
+@pytest.mark.parametrize("n,widths", [(8, (0, 4)), (15, (0, 5, 6, 7))])
+def test_fusion_mode_same_answers(A, n, widths):
+    """The drop-in API gives the same probabilities fused (CUDA cores at 8
+    qubits; the tensor cores at 15, up to 7-qubit blocks) as per gate."""
+    for k in widths:
+        c = A.qc_create_ex(n, capi.C64, capi.PHYSICAL, k)
         A.qc_quantum_fourier_transform(c)
-        for q in range(8):
+        for q in range(n):
             A.qc_rx(c, q, 0.1 * q)
         A.qc_ghz_state(c)
-        p = [A.qc_get_probability(c, i) for i in range(256)]
+        for q in range(0, n - 1, 2):
+            A.qc_cnot(c, q, q + 1)
+            A.qc_ry(c, q + 1, 0.3)
+        p = np.array([A.qc_get_probability(c, i) for i in range(1 << n)])
         if k == 0:
             ref = p
         else:
