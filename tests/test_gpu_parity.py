@@ -542,7 +542,7 @@ def _inverse(g: W.GateList) -> W.GateList:
 
 
 @pytest.mark.parametrize("fusion_k,engine", [(0, capi.FUSE_AUTO), (4, capi.FUSE_SIMT),
-                                             (6, capi.FUSE_TENSOR)])
+                                             (6, capi.FUSE_TENSOR), (7, capi.FUSE_TENSOR)])
 def test_30q_brick_then_inverse_returns_to_zero(fusion_k, engine):
     n = 30
     g = W.brick_circuit(n, 3, 5)
