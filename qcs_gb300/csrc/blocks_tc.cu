@@ -40,6 +40,9 @@
 // block matrix (hi + lo) + tables, the column-norm ring and the low-mode
 // staging = 215 KB.  HBM traffic: one read and one write of the state per
 // block; tensor work per amplitude 3 x 8 x 2^k flops.
+//
+// k = 7 does not fit this layout (its real form alone would take 256 KB):
+// k_block_tc7 keeps the real and imaginary parts apart (Tc7, below).
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdlib.h>
