@@ -158,6 +158,7 @@ struct TcGeom {
   i64 col_off[kTcM];  // column m -> offset (bits of m on the column qubits)
   i64 blk_off[128];   // block index a -> offset (bit j of a on qubits[j])
   i64 run_off[128];   // piece j -> offset of its first amplitude
+  i64 nib[10][16];    // tile id nibble k with value v -> its part of the tile's offset
 };
 
 // Prefetch shape, measured at 30 qubits over six k = 6 block placements
@@ -171,9 +172,12 @@ struct TcGeom {
 static int pf_ahead(int k) { return k == 7 ? 1 : 2; }
 static int pf_piece_bits() { return 16; }
 
+// The tile's offset: its id's bits scattered onto the free qubits, four
+// bits per table lookup (the index is the same across a warp, so the
+// parameter-space reads broadcast).
 __device__ __forceinline__ i64 tile_base(i64 tile, const TcGeom &g) {
   i64 b = 0;
-  for (int j = 0; j < g.nfree; j++) b |= ((tile >> j) & 1LL) << g.freeq[j];
+  for (int k = 0; 4 * k < g.nfree; k++) b += g.nib[k][(tile >> (4 * k)) & 15];
   return b;
 }
 
@@ -684,9 +688,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     float partl[LSTEPS];       // kLowMode: per-step column norms over a tile
     const TileWalk w = tile_walk(g);
     const i64 nq = (i64)S::CHUNKS * w.count;  // chunks, an even number
+    i64 load_tile = -1, load_base = 0;  // the tile base, computed once per tile
     auto load_chunk = [&](auto bc, i64 q) {
       constexpr int b = decltype(bc)::value;
-      const i64 base = tile_base(w.at(q / S::CHUNKS), g);
+      if (q / S::CHUNKS != load_tile) {
+        load_tile = q / S::CHUNKS;
+        load_base = tile_base(w.at(load_tile), g);
+      }
+      const i64 base = load_base;
       const int c = (int)(q % S::CHUNKS);
       if constexpr (MODE == kLowMode) {
 #pragma unroll
@@ -1189,6 +1198,13 @@ static void tc_prepare(const qcs_cuda_state *s, int k, const int *qubits_in, con
     }
   for (int q = 0; q < s->n; q++)
     if (role[q] == -1) g.freeq[g.nfree++] = (signed char)q;
+  for (int k = 0; 4 * k < g.nfree; k++)
+    for (int v = 0; v < 16; v++) {
+      i64 o = 0;
+      for (int b = 0; b < 4 && 4 * k + b < g.nfree; b++)
+        if ((v >> b) & 1) o |= 1LL << g.freeq[4 * k + b];
+      g.nib[k][v] = o;
+    }
   g.n_tiles = 1LL << g.nfree;
   for (int m = 0; m < kTcM; m++) {
     i64 o = 0;
