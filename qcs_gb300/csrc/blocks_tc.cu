@@ -128,21 +128,26 @@ struct Tc7 {
   static constexpr int N = KA;                     // UMMA N: outputs of one part
   static constexpr int CH_BYTES = kTcM * KC * 2;   // one bf16 chunk operand
   static constexpr int U_BYTES = N * KA * 2;       // one bf16 matrix operand
-  static constexpr int UPT = kTcM * KC / 8 / kTcProdThreads;  // 8-amplitude units per producer
+  static constexpr int PROD_WARPS = 16;            // producer warps (k_block_tc has 8)
+  static constexpr int PROD_THREADS = 32 * PROD_WARPS;
+  static constexpr int MMA_WARP = kTcEpiWarps + PROD_WARPS;
+  static constexpr int THREADS = 32 * (MMA_WARP + 1);
+  static constexpr int SQ_PARTS = PROD_THREADS / kTcM;   // producers per column
+  static constexpr int UPT = kTcM * KC / 8 / PROD_THREADS;  // 8-amplitude units per producer
   static constexpr int TMEM_COLS = 512;            // [stage][re, im][N]
   static constexpr int OFF_A = 0;                  // [stage][re hi, re lo, im hi, im lo][CH_BYTES]
   static constexpr int OFF_B = 8 * CH_BYTES;       // [re hi, re lo, im hi, im lo][U_BYTES]
   static constexpr int OFF_COL = OFF_B + 4 * U_BYTES;
   static constexpr int OFF_BLK = OFF_COL + kTcM * 8;
-  static constexpr int OFF_SQ = OFF_BLK + KA * 8;  // float [slot 4][half][column]
-  static constexpr int OFF_BETA = OFF_SQ + kSqSlots * 2 * kTcM * 4;  // float2[KA]
+  static constexpr int OFF_SQ = OFF_BLK + KA * 8;  // float [slot 4][part][column]
+  static constexpr int OFF_BETA = OFF_SQ + kSqSlots * SQ_PARTS * kTcM * 4;  // float2[KA]
   static constexpr int OFF_EPI = OFF_BETA + KA * 8;  // kLowMode staging
   static constexpr int OFF_BAR = OFF_EPI + kTcEpiWarps * 32 * kEpiPitch * 4;
   static constexpr int OFF_MISC = OFF_BAR + 16 * 8;
   static constexpr int SMEM = OFF_MISC + 16 + 1024;
   static constexpr int IMG_BYTES = 4 * U_BYTES;
   static_assert(SMEM <= 232448, "exceeds the 227 KB shared-memory opt-in");
-  static_assert(UPT == 2 && CHUNKS % 2 == 0, "producer shares and stage pairs");
+  static_assert(UPT == 1 && CHUNKS % 2 == 0, "producer shares and stage pairs");
 };
 
 // An upload slot: the largest (k = 7) image, then the block's row sums (float2).
@@ -595,20 +600,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }
 
 // k = 7 (the complex form, Tc7).  Same roles, waits and fused epilogue as
-// k_block_tc; what differs is the operand layout and the chunked pipeline:
+// k_block_tc, with 16 producer warps instead of 8 (672 threads, 80
+// registers a thread); what differs is the operand layout and the chunked
+// pipeline:
 //   producers  convert chunk q (tile q / 4, amplitudes 32 (q % 4) ..) into
 //              stage q % 2 once the MMAs of chunk q - 2 are done, holding
 //              chunks q + 1 and q + 2 in flight in registers meanwhile;
 //   MMA        12 products per 16-amplitude K-step (Re, Im x 3 split terms x
 //              2 parts), committing a stage back after every chunk and the
 //              accumulator pair after a tile's last chunk;
-//   epilogue   reads Re and Im of 32 outputs at a time (two tcgen05.ld).
+//   epilogue   reads Re and Im of 16 outputs at a time, both loads under
+//              one completion wait.
 // In kLowMode (the block is qubits 0..6) a column is 128 adjacent
 // amplitudes: a producer warp instruction reads 256 contiguous bytes of each
 // of 2 columns, and the epilogue transposes 32 x 16 results through shared
 // memory, as in k_block_tc.
 template <int MODE, bool FUSED>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(Tc7::THREADS, 1)
     k_block_tc7(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
                 const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err) {
   using S = Tc7;
@@ -631,8 +639,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
-    mbar_init(bar(0), kTcProdThreads);
-    mbar_init(bar(1), kTcProdThreads);
+    mbar_init(bar(0), S::PROD_THREADS);
+    mbar_init(bar(1), S::PROD_THREADS);
     mbar_init(bar(2), 1);
     mbar_init(bar(3), 1);
     mbar_init(bar(4), 1);
@@ -640,28 +648,28 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     mbar_init(bar(6), kTcEpiThreads);
     mbar_init(bar(7), kTcEpiThreads);
     mbar_init(bar(8), 1);
-    for (int k = 0; k < kSqSlots; k++) mbar_init(bar(9 + k), kTcProdThreads);
+    for (int k = 0; k < kSqSlots; k++) mbar_init(bar(9 + k), S::PROD_THREADS);
     *abort_flag = 0;
     fence_barrier_init();
   }
-  for (int i = tid; i < kTcM; i += kTcThreads) col_off[i] = g.col_off[i];
-  for (int i = tid; i < S::KA; i += kTcThreads) blk_off[i] = g.blk_off[i];
+  for (int i = tid; i < kTcM; i += S::THREADS) col_off[i] = g.col_off[i];
+  for (int i = tid; i < S::KA; i += S::THREADS) blk_off[i] = g.blk_off[i];
   {
     uint4 *dst = reinterpret_cast<uint4 *>(sB);
-    for (int i = tid; i < S::IMG_BYTES / 16; i += kTcThreads) dst[i] = bimg[i];
+    for (int i = tid; i < S::IMG_BYTES / 16; i += S::THREADS) dst[i] = bimg[i];
   }
   float2 *beta = reinterpret_cast<float2 *>(smem + S::OFF_BETA);
   if (FUSED && diffuse_sum) {  // as in k_block_tc: beta[a] = 2m * (row sum a of U)
     const float tr = (float)(2.0 * (diffuse_sum[0] * inv_n));
     const float ti = (float)(2.0 * (diffuse_sum[1] * inv_n));
     const float2 *rows = reinterpret_cast<const float2 *>(bimg + S::IMG_BYTES / 16);
-    for (int i = tid; i < S::KA; i += kTcThreads) {
+    for (int i = tid; i < S::KA; i += S::THREADS) {
       const float2 r = rows[i];
       beta[i] = make_float2(tr * r.x - ti * r.y, tr * r.y + ti * r.x);
     }
   }
   fence_async_shared();
-  if (warp == kTcMmaWarp) {
+  if (warp == S::MMA_WARP) {
     tmem_alloc(smem_u32(tmem_slot), S::TMEM_COLS);
     tmem_relinquish();
   }
@@ -670,7 +678,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp >= kTcEpiWarps && warp < kTcMmaWarp) {
+  if (warp >= kTcEpiWarps && warp < S::MMA_WARP) {
     // ---------------- producers ----------------
     // Thread p keeps column mc = p % 128; of a chunk's 4 units of 8
     // amplitudes it takes units p / 128 and p / 128 + 2.  Chunk q's
@@ -682,7 +690,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int p = tid - kTcEpiThreads;
     const int mc = p & (kTcM - 1);
     const int pw = p >> 5;
-    constexpr int LSTEPS = kTcM / (2 * kTcProdWarps);  // kLowMode: 2-column steps per chunk
+    constexpr int LSTEPS = kTcM / (2 * S::PROD_WARPS);  // kLowMode: 2-column steps per chunk
     float2 xc[2][S::UPT][8];   // other modes: [chunk parity][unit][amplitude]
     float4 xl[2][LSTEPS];      // kLowMode: [chunk parity][step]
     float partl[LSTEPS];       // kLowMode: per-step column norms over a tile
@@ -708,7 +716,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const float2 *src = v + base + col_off[mc];
 #pragma unroll
         for (int i = 0; i < S::UPT; i++) {
-          const int a = c * S::KC + 8 * ((p >> 7) + 2 * i);
+          const int a = c * S::KC + 8 * ((p >> 7) + S::SQ_PARTS * i);
           if constexpr (MODE == kPairMode) {
 #pragma unroll
             for (int e = 0; e < 8; e += 2) {
@@ -754,7 +762,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       } else {
 #pragma unroll
         for (int i = 0; i < S::UPT; i++) {
-          const int j = (p >> 7) + 2 * i;
+          const int j = (p >> 7) + S::SQ_PARTS * i;
           uint32_t wd[4][4];  // [re hi, re lo, im hi, im lo][pair of amplitudes]
 #pragma unroll
           for (int e = 0; e < 8; e += 2) {
@@ -774,7 +782,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // the tile's column norms into slot it % 4: kLowMode sums each column's
     // 16 lanes (fixed order); otherwise threads p and p + 128 hold the halves
     auto store_norms = [&](i64 it) {
-      float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
+      float *sq = colsq + (it % kSqSlots) * S::SQ_PARTS * kTcM;
       if constexpr (MODE == kLowMode) {
 #pragma unroll
         for (int i = 0; i < LSTEPS; i++) {
@@ -784,11 +792,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           if ((lane & 15) == 0) {
             const int m = pw * 2 * LSTEPS + 2 * i + (lane >> 4);
             sq[m] = x;
-            sq[kTcM + m] = 0.f;
+#pragma unroll
+            for (int h = 1; h < S::SQ_PARTS; h++) sq[h * kTcM + m] = 0.f;
           }
         }
       } else {
-        sq[(p >> 7) * kTcM + mc] = part;
+        sq[(p >> 7) * kTcM + mc] = part;  // part p / 128 of column mc's norm
       }
     };
     // one chunk: false when the CTA is aborting
@@ -823,7 +832,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     for (i64 q = 0; q < nq; q += 2)
       if (!step(b0, q) || !step(b1, q + 1)) break;
-  } else if (warp == kTcMmaWarp) {
+  } else if (warp == S::MMA_WARP) {
     // ---------------- MMA issue ----------------
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(kTcM, S::N);
@@ -907,31 +916,33 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (renorm) {
         float out = 0.f;
 #pragma unroll 1
-        for (int cc = 0; cc < 2 * S::N / 64; cc++) {  // Re then Im: adjacent columns
-          float acc[64];
-          tmem_ld64(tr + 64 * cc, acc);
+        for (int cc = 0; cc < 2 * S::N / 32; cc++) {  // Re then Im: adjacent columns
+          float acc[32];  // 32 columns a wait: 21 warps leave 80 registers a thread
+          tmem_ld16x2(tr + 32 * cc, tr + 32 * cc + 16, acc, acc + 16);
 #pragma unroll
-          for (int q = 0; q < 64; q++) out += acc[q] * acc[q];
+          for (int q = 0; q < 32; q++) out += acc[q] * acc[q];
         }
-        const float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
-        const float in = sq[m] + sq[kTcM + m];
+        const float *sq = colsq + (it % kSqSlots) * S::SQ_PARTS * kTcM;
+        float in = 0.f;
+#pragma unroll
+        for (int h = 0; h < S::SQ_PARTS; h++) in += sq[h * kTcM + m];
         if (out > 0.f) scale = sqrtf(in / out);
       }
       const i64 tbase = tile_base(tile, g);
       float2 *dst = v + tbase + col_off[m];
+      // 16 outputs at a time: 21 warps leave 80 registers a thread
 #pragma unroll 1
-      for (int gq = 0; gq < S::N / 32; gq++) {
-        float re[32], im[32];
-        tmem_ld32(tr + 32 * gq, re);
-        tmem_ld32(ti + 32 * gq, im);
+      for (int gq = 0; gq < S::N / 16; gq++) {
+        float re[16], im[16];
+        tmem_ld16x2(tr + 16 * gq, ti + 16 * gq, re, im);
         float pr = 0.f, pi = 0.f;
 #pragma unroll
-        for (int q = 0; q < 32; q++) {
+        for (int q = 0; q < 16; q++) {
           re[q] *= scale;
           im[q] *= scale;
           if constexpr (FUSED) {
             if (diffuse_sum) {
-              const float2 b = beta[32 * gq + q];
+              const float2 b = beta[16 * gq + q];
               re[q] = b.x - re[q];
               im[q] = b.y - im[q];
             }
@@ -946,34 +957,30 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
         }
         if constexpr (MODE == kLowMode) {
-          // 32 columns x 16 outputs at a time through the warp's staging rows;
-          // then lanes 0-15 store column j and lanes 16-31 column j + 1, one
+          // 32 columns x 16 outputs through the warp's staging rows; then
+          // lanes 0-15 store column j and lanes 16-31 column j + 1, one
           // amplitude each: two full 128-byte lines per instruction
           float *buf = epi + warp * 32 * kEpiPitch;
           const int half = lane >> 4, row = lane & 15;
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
-#pragma unroll
-            for (int q = 0; q < 16; q++)
-              *reinterpret_cast<float2 *>(buf + lane * kEpiPitch + 2 * q) =
-                  make_float2(re[16 * h + q], im[16 * h + q]);
-            __syncwarp();
+          for (int q = 0; q < 16; q++)
+            *reinterpret_cast<float2 *>(buf + lane * kEpiPitch + 2 * q) = make_float2(re[q], im[q]);
+          __syncwarp();
 #pragma unroll 4
-            for (int j = 0; j < 32; j += 2) {
-              const float2 val =
-                  *reinterpret_cast<const float2 *>(buf + (j + half) * kEpiPitch + 2 * row);
-              v[tbase + col_off[warp * 32 + j + half] + 32 * gq + 16 * h + row] = val;
-            }
-            __syncwarp();
+          for (int j = 0; j < 32; j += 2) {
+            const float2 val =
+                *reinterpret_cast<const float2 *>(buf + (j + half) * kEpiPitch + 2 * row);
+            v[tbase + col_off[warp * 32 + j + half] + 16 * gq + row] = val;
           }
+          __syncwarp();
         } else if constexpr (MODE == kPairMode) {
 #pragma unroll
-          for (int q = 0; q < 32; q += 2)
-            *reinterpret_cast<float4 *>(dst + blk_off[32 * gq + q]) =
+          for (int q = 0; q < 16; q += 2)
+            *reinterpret_cast<float4 *>(dst + blk_off[16 * gq + q]) =
                 make_float4(re[q], im[q], re[q + 1], im[q + 1]);
         } else {
 #pragma unroll
-          for (int q = 0; q < 32; q++) dst[blk_off[32 * gq + q]] = make_float2(re[q], im[q]);
+          for (int q = 0; q < 16; q++) dst[blk_off[16 * gq + q]] = make_float2(re[q], im[q]);
         }
       }
       tc_fence_before();
@@ -998,7 +1005,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
   tc_fence_before();
   __syncthreads();
-  if (warp == kTcMmaWarp) {
+  if (warp == S::MMA_WARP) {
     tc_fence_after();
     tmem_dealloc(tmem, S::TMEM_COLS);
   }
@@ -1091,10 +1098,10 @@ static int launch_tc7(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int 
   const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
   prof_begin(s);
   if (diffuse_sum || sum_out)
-    k_block_tc7<MODE, true><<<grid, kTcThreads, Tc7::SMEM, s->stream>>>(
+    k_block_tc7<MODE, true><<<grid, Tc7::THREADS, Tc7::SMEM, s->stream>>>(
         (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err);
   else
-    k_block_tc7<MODE, false><<<grid, kTcThreads, Tc7::SMEM, s->stream>>>(
+    k_block_tc7<MODE, false><<<grid, Tc7::THREADS, Tc7::SMEM, s->stream>>>(
         (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err);
   return launched(s, KC_BLOCK_TC7, 2.0 * s->size * 8.0, "apply_block (tcgen05, k = 7)");
 }
