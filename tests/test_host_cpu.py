@@ -108,7 +108,7 @@ def test_plan_keeps_non_gate_ops_as_barriers():
 def test_plan_block_counts_brick30():
     """Wider blocks mean fewer passes over the state; width 7 (the widest the
     tensor cores take) plans the headline circuit in 51 blocks against 63 at
-    width 6, and widths above 7 plan as 7."""
+    width 6, and the planner caps wider requests at 7."""
     g = W.brick_circuit(30, 40, 1)
     counts = [capi.plan(g, 30, k)[2] for k in (2, 4, 6, 7, 8)]
     assert counts[0] > counts[1] > counts[2] > counts[3] == counts[4]
