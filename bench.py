@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--engine", default=os.environ.get("QCS_BENCH_ENGINE", "auto"),
                     choices=["auto", "simt", "tensor"])
     ap.add_argument("--plain-steps", type=int, default=None,
-                    help="timed steps of the plain form (default: --steps)")
+                    help="timed steps of the plain form (default: --steps, at most 3: "
+                         "one plain step is ~10 s)")
     ap.add_argument("--parity-qubits", type=int, default=24)
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--cpu-sample-gates", type=int, default=48)
@@ -59,11 +60,12 @@ def parse():
     ap.add_argument("--only", default=None,
                     help="with --sweeps: comma-separated subset of sweep types")
     ap.add_argument("--workload", default="brick",
-                    choices=["brick", "random20", "grover", "batch", "learned"],
+                    choices=["brick", "random20", "grover", "batch", "learned", "shards"],
                     help="brick: the headline 30-qubit brick circuit; random20: 20-qubit "
                          "complex128 QFT + 200 random gates vs the reference rule; grover: "
                          "QFT + 64 Grover iterations at --qubits (33/34); batch: 4096 "
-                         "variational instances in one persistent launch")
+                         "variational instances in one persistent launch; shards: launch "
+                         "check, every rank reports its share of the batch (no GPU work)")
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--no-autotune", action="store_true",
                     help="batch: keep the default schedule (512 threads, tile 2^13, 2 CTAs/SM)")
@@ -230,6 +232,14 @@ def infidelity(a, b) -> float:
     return float(1.0 - abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real))
 
 
+def host_threads() -> int:
+    """Host threads this process may run on."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def cpu_sample(gates, n: int, count: int, mode: int):
     """Time the oracle on the first `count` gates of the workload at n qubits.
     Returns (gate-apps/s, seconds, threads)."""
@@ -237,8 +247,8 @@ def cpu_sample(gates, n: int, count: int, mode: int):
     sub = type(gates)()
     for k, t, c, a in list(zip(gates.kinds, gates.targets, gates.controls, gates.angles))[:count]:
         sub.add(k, t, c, a)
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    threads = host_threads()
+    O.set_threads(threads)  # a launcher may have set OMP_NUM_THREADS=1
     with O.OracleState(n, mode) as s:
         t0 = time.perf_counter()
         s.run(sub)
@@ -246,8 +256,20 @@ def cpu_sample(gates, n: int, count: int, mode: int):
     return len(sub) / dt, dt, threads
 
 
+def headline_config(args, world: int, gates: int) -> dict:
+    """The workload of the headline line, identical in both arms."""
+    return {"workload": WORKLOAD, "qubits": args.qubits, "depth": args.depth, "gates": gates,
+            "seed": args.seed, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (8 GiB state vs 129 MB), no flush"}
+
+
 def run_reference(args, dist):
-    """--impl reference: the CPU restatement of the reference's algorithm."""
+    """--impl reference: the CPU restatement of the reference's algorithm.
+
+    Each step is a bounded sample of the workload: its first
+    --cpu-sample-gates gates.  `ms_per_step` is the time of that sample as
+    measured; the time the whole circuit would take at that rate is a separate
+    key, `extrapolated_to_full_step_ms`."""
     if dist.rank != 0:
         return
     from oracle import oracle as O
@@ -260,6 +282,7 @@ def run_reference(args, dist):
     for _ in range(args.warmup):
         cpu_sample(gates, n_cpu, max(4, count // 8), O.COMPAT)
     times = []
+    threads = 1
     for _ in range(args.steps):
         rate, dt, threads = cpu_sample(gates, n_cpu, count, O.COMPAT)
         times.append(dt)
@@ -270,11 +293,12 @@ def run_reference(args, dist):
               + ("" if scale == 1.0 else f", rate scaled by 2^{n_cpu - args.qubits} amplitudes"))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": dt * 1e3 * (len(gates) / count) / scale,
+            "ms_per_step": dt * 1e3,
+            "step": f"one sample: the first {count} of {len(gates)} gates",
+            "extrapolated_to_full_step_ms": dt * 1e3 * (len(gates) / count) / scale,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "complex128", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "qubits": args.qubits, "depth": args.depth,
-                       "gates": len(gates), "seed": args.seed},
+            "config": headline_config(args, args.gpus, len(gates)),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -312,6 +336,28 @@ def time_form(state, ops, k, engine, steps, warmup, dist, profile=True):
     return dist.max(ms), launches, prof
 
 
+def time_e2e(state, ops, k, engine, steps, dist, draws, plan_cache):
+    """Host wall clock of `steps` end-to-end steps through the C ABI: reset to
+    |0...0>, run the op list from host memory, sample the host draws, read
+    the argmax.  Returns (seconds over ranks, h2d bytes/step, d2h bytes/step)
+    from the library's own transfer counters."""
+    state.set_basis(0)
+    state.run(ops, fusion_k=k, engine=engine, plan_cache=plan_cache)
+    state.sample(draws)
+    state.synchronize()
+    dist.barrier()
+    x0 = state.transfer_bytes()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        state.set_basis(0)
+        state.run(ops, fusion_k=k, engine=engine, plan_cache=plan_cache)
+        state.sample(draws)
+        state.argmax()
+    dt = dist.max(time.perf_counter() - t0)
+    x1 = state.transfer_bytes()
+    return dt, (x1[0] - x0[0]) // steps, (x1[1] - x0[1]) // steps
+
+
 def run_ours(args, dist):
     from qcs_gb300 import build as B
     from qcs_gb300 import capi
@@ -325,7 +371,7 @@ def run_ours(args, dist):
     G = len(gates)
     state = capi.State(n, capi.C64)
     peaks = measured_peaks()
-    plain_steps = args.plain_steps if args.plain_steps is not None else args.steps
+    plain_steps = args.plain_steps if args.plain_steps is not None else min(args.steps, 3)
 
     with ClockSampler(0) as clk:
         fused_ms, launches, prof = time_form(state, ops, args.fusion_k, engine, args.steps,
@@ -335,32 +381,23 @@ def run_ours(args, dist):
     clocks = clk.summary()
 
     # end to end through the C ABI with host buffers: gate list from host
-    # memory, 1024 shot draws uploaded, the samples and the argmax read back
+    # memory, 1024 shot draws uploaded, the samples and the argmax read back.
+    # Two forms: the state's kept plan (a circuit run again: its tensor-core
+    # blocks stay on the device), and the plan cache off, so that every step
+    # also plans the circuit, forms its block matrices in FP64 on the host
+    # and uploads their images (a circuit seen for the first time).
     shots = 1024
     draws = np.random.default_rng(args.seed).random(shots)
-    for _ in range(1):
-        state.set_basis(0)
-        state.run(ops, fusion_k=args.fusion_k, engine=engine)
-        state.sample(draws)
-    state.synchronize()
-    dist.barrier()
-    x0 = state.transfer_bytes()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        state.set_basis(0)
-        state.run(ops, fusion_k=args.fusion_k, engine=engine)
-        samples = state.sample(draws)
-        top = state.argmax()
-    e2e_s = dist.max(time.perf_counter() - t0)
-    x1 = state.transfer_bytes()
-    h2d_step = (x1[0] - x0[0]) // args.steps
-    d2h_step = (x1[1] - x0[1]) // args.steps
-    del samples, top
+    e2e_s, h2d_step, d2h_step = time_e2e(state, ops, args.fusion_k, engine, args.steps, dist,
+                                         draws, plan_cache=True)
+    fresh_s, fresh_h2d, fresh_d2h = time_e2e(state, ops, args.fusion_k, engine, args.steps,
+                                             dist, draws, plan_cache=False)
 
     world = dist.world
     value = world * G * args.steps / (fused_ms / 1e3)
     plain_value = world * G * plain_steps / (plain_ms / 1e3)
     e2e_value = world * G * args.steps / e2e_s
+    fresh_value = world * G * args.steps / fresh_s
 
     # dominant kernel of the fused form
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
@@ -388,12 +425,13 @@ def run_ours(args, dist):
         O.build()
         pn = cpu_qubits(args.parity_qubits, buffers=1)
         pg = W.brick_circuit(pn, args.depth, args.seed)
+        threads = host_threads()
+        O.set_threads(threads)
         t0 = time.perf_counter()
         with O.OracleState(pn) as o:
             o.run(pg)
             ref = o.amplitudes()
         cpu_dt = time.perf_counter() - t0
-        threads = os.cpu_count() or 1
         with capi.State(pn, capi.C64) as s:
             s.run(pg.ops(), fusion_k=args.fusion_k, engine=engine)
             a = s.amplitudes()
@@ -418,12 +456,13 @@ def run_ours(args, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": fused_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "complex64 (fp32 math)",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "complex64 state; fused blocks: split-BF16x3 tensor products, FP32 accumulate",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "qubits": n, "depth": args.depth, "gates": G,
-                   "seed": args.seed, "form": "fused", "fusion_k": args.fusion_k,
-                   "engine": args.engine, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (8 GiB state vs 129 MB), no flush"},
+        "config": headline_config(args, world, G),
+        "form": {"name": "fused", "fusion_k": args.fusion_k, "engine": args.engine,
+                 "partitioner": "greedy", "plan_cache": "kept plan (value, e2e); "
+                 "plan cache off (e2e_fresh)"},
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms / plain_steps,
                   "steps": plain_steps, "gpu_launches": plain_launches,
                   "hbm_gbs_by_kernel": sweep_gbs},
@@ -439,8 +478,17 @@ def run_ours(args, dist):
                 "bytes_source": "the library's own transfer counters (qcs_cuda_transfer_bytes): "
                                 "block-matrix images, 2x2 gate matrices, shot draws up; "
                                 "samples and results down",
+                "plan_cache": "on: the state's kept plan (blocks resident on the device)",
                 "path": "qcs_cuda_set_basis + qcs_cuda_run(host op list) + "
                         "qcs_cuda_sample(1024 host draws) + qcs_cuda_argmax, host wall clock"},
+        "e2e_fresh": {"value": fresh_value, "unit": UNIT,
+                      "h2d_bytes_per_step": int(fresh_h2d),
+                      "d2h_bytes_per_step": int(fresh_d2h),
+                      "over_e2e": fresh_value / e2e_value,
+                      "plan_cache": "off (QCS_RUN_NO_PLAN_CACHE): every step plans the "
+                                    "circuit, forms its block matrices and uploads their "
+                                    "images",
+                      "path": "as e2e"},
         "gpu_launches": launches,
     }
     state.close()
@@ -842,11 +890,52 @@ def run_learned(args, dist):
     print(json.dumps(line), flush=True)
 
 
+def relaunch(args):
+    """`--gpus N` (N > 1) outside a launcher: start N ranks of this same
+    command under torch.distributed.run on 127.0.0.1, one process per GPU,
+    and return their exit status.  None when this process is a rank already
+    (WORLD_SIZE set) or N == 1."""
+    if args.gpus <= 1 or "WORLD_SIZE" in os.environ:
+        return None
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           f"--nproc-per-node={args.gpus}", "--master-addr", "127.0.0.1",
+           "--master-port", str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
+def run_shards(args, dist):
+    """Launch check (no GPU work): every rank takes its round-robin share of
+    the batched workload's instances; rank 0 gathers the shares and the
+    ranks' process ids over the host process group and prints them."""
+    from qcs_gb300 import workloads as W
+    inst = W.variational_batch(args.instances, args.seed)
+    mine = shard(list(range(len(inst))), dist)
+    mine_q = [inst[i][0] for i in mine]
+    rec = {"rank": dist.rank, "pid": os.getpid(), "instances": mine, "qubits": mine_q}
+    if dist.world > 1:
+        got = [None] * dist.world
+        dist.td.all_gather_object(got, rec)
+    else:
+        got = [rec]
+    if dist.rank == 0:
+        print(json.dumps({"mode": "shards", "n_gpus": dist.world, "instances": len(inst),
+                          "ranks": got}), flush=True)
+
+
 def main():
     args = parse()
+    rc = relaunch(args)
+    if rc is not None:
+        sys.exit(rc)
     dist = Dist()
     try:
-        if args.sweeps:
+        if args.workload == "shards":
+            run_shards(args, dist)
+        elif args.sweeps:
             run_sweeps(args, dist)
         elif args.workload == "random20":
             run_random20(args, dist)

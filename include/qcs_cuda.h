@@ -342,9 +342,9 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
 
 /* Shot sampling that allocates no memory (no counterpart in the reference).
  * For callers that cannot call cudaMalloc where they sample: a host
- * application that owns all device memory through its own pool, a
+ * application that owns all device memory through its own pool, or a
  * latency-critical loop that must not take cudaMalloc's implicit device
- * synchronisation, or code preparing work while a stream is being captured.
+ * synchronisation.
  * Same draws-to-indices rule as qcs_cuda_sample, but every pointer is a
  * device pointer the caller provides: `amplitudes` (count complex64 or
  * complex128 values, precision QCS_CUDA_C64 / QCS_CUDA_C128), `draws`
@@ -354,8 +354,10 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
  * Limit: count must be a power of two no larger than 2^28 amplitudes; the
  * scratch is a fixed 512 KB array inside the library, held on every GPU that
  * loads it until the process exits.  The first call on a device looks up
- * that array's device address and should come before any stream capture.
- * Calls share the array: two calls that overlap on the GPU race. */
+ * that array's device address and should come before any stream capture;
+ * a device reset invalidates it (a call whose launch fails looks it up
+ * again on the next call).  Calls share the array: two calls that overlap
+ * on the GPU race. */
 int qcs_cuda_sample_noalloc(const void *amplitudes, long long count,
                             int precision, const double *draws, int shots,
                             long long *samples, void *stream);

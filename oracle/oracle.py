@@ -23,6 +23,13 @@ COMPAT = 1
 _lib = None
 
 
+def ref_sources_present() -> bool:
+    """Whether the reference's sources are where the Makefile reads them
+    (``make ref-present``)."""
+    return subprocess.run(["make", "-s", "-C", HERE, "ref-present"],
+                          stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL).returncode == 0
+
+
 def build(ref: bool = False) -> None:
     """Compile liboracle.so (and the reference libraries when ``ref``).
     Libraries built on another machine type are rebuilt."""

@@ -166,36 +166,122 @@ std::vector<PlanItem> partition(const qcs_cuda_op *ops, int count, int n,
   return plan;
 }
 
+// U := G U for one gate, on the rows (a, a | tb) of every control setting.
+// U is held as separate real and imaginary planes (row-major K x K), so the
+// column loops are plain FP64 streams.  Only the columns that can be nonzero
+// are visited: starting from the identity, after gates on the block bits in
+// `touched`, U[a][c] = 0 unless a and c agree outside `touched`.  Three gate
+// shapes: diagonal (Z, P, RZ, CPHASE: each row scaled, rows equal to 1 left
+// alone), exchange (X, Y, CNOT: rows swapped and scaled) and dense.  Each
+// element is computed as g00*v0 + g01*v1 with the zero terms of the first
+// two shapes left out, which changes no value (at most the sign of a zero).
+struct Planes {
+  int K;
+  std::vector<double> re, im;
+};
+
+static inline void cmul_into(double gr, double gi, double vr, double vi, double &or_, double &oi) {
+  or_ = gr * vr - gi * vi;
+  oi = gr * vi + gi * vr;
+}
+
+static void apply_gate_planes(Planes &P, const double m[8], int tb, int cb, int touched) {
+  const int K = P.K;
+  const bool diag = m[2] == 0.0 && m[3] == 0.0 && m[4] == 0.0 && m[5] == 0.0;
+  const bool exch = m[0] == 0.0 && m[1] == 0.0 && m[6] == 0.0 && m[7] == 0.0;
+  const bool full = touched == K - 1;  // every column may be nonzero
+  const int free_mask = (K - 1) & ~touched;
+  for (int a = 0; a < K; a++) {
+    if (a & tb) continue;
+    if (cb && !(a & cb)) continue;
+    double *r0r = &P.re[(size_t)a * K], *r0i = &P.im[(size_t)a * K];
+    double *r1r = &P.re[(size_t)(a | tb) * K], *r1i = &P.im[(size_t)(a | tb) * K];
+    // the columns to visit: c = (a & free_mask) | sub for every subset sub
+    // of `touched` (all K columns once every bit is touched)
+    const int cbase = a & free_mask;
+    auto each_col = [&](auto &&f) {
+      if (full) {
+        for (int c = 0; c < K; c++) f(c);
+      } else {
+        int sub = 0;
+        do {
+          f(cbase | sub);
+          sub = (sub - touched) & touched;
+        } while (sub != 0);
+      }
+    };
+    if (diag) {
+      const bool one0 = m[0] == 1.0 && m[1] == 0.0, one1 = m[6] == 1.0 && m[7] == 0.0;
+      if (!one0)
+        each_col([&](int c) {
+          double xr, xi;
+          cmul_into(m[0], m[1], r0r[c], r0i[c], xr, xi);
+          r0r[c] = xr;
+          r0i[c] = xi;
+        });
+      if (!one1)
+        each_col([&](int c) {
+          double xr, xi;
+          cmul_into(m[6], m[7], r1r[c], r1i[c], xr, xi);
+          r1r[c] = xr;
+          r1i[c] = xi;
+        });
+    } else if (exch) {
+      const bool swap_only = m[2] == 1.0 && m[3] == 0.0 && m[4] == 1.0 && m[5] == 0.0;
+      each_col([&](int c) {
+        const double v0r = r0r[c], v0i = r0i[c], v1r = r1r[c], v1i = r1i[c];
+        if (swap_only) {
+          r0r[c] = v1r;
+          r0i[c] = v1i;
+          r1r[c] = v0r;
+          r1i[c] = v0i;
+        } else {
+          cmul_into(m[2], m[3], v1r, v1i, r0r[c], r0i[c]);
+          cmul_into(m[4], m[5], v0r, v0i, r1r[c], r1i[c]);
+        }
+      });
+    } else {
+      each_col([&](int c) {
+        const double v0r = r0r[c], v0i = r0i[c], v1r = r1r[c], v1i = r1i[c];
+        double ar, ai, br, bi;
+        cmul_into(m[0], m[1], v0r, v0i, ar, ai);
+        cmul_into(m[2], m[3], v1r, v1i, br, bi);
+        r0r[c] = ar + br;
+        r0i[c] = ai + bi;
+        cmul_into(m[4], m[5], v0r, v0i, ar, ai);
+        cmul_into(m[6], m[7], v1r, v1i, br, bi);
+        r1r[c] = ar + br;
+        r1i[c] = ai + bi;
+      });
+    }
+  }
+}
+
 void block_matrix(const qcs_cuda_op *ops, const PlanItem &item, std::vector<cd> &u) {
   const int k = (int)item.qubits.size();
   const int K = 1 << k;
-  u.assign((size_t)K * K, cd(0.0, 0.0));
-  for (int a = 0; a < K; a++) u[(size_t)a * K + a] = cd(1.0, 0.0);
+  Planes P;
+  P.K = K;
+  P.re.assign((size_t)K * K, 0.0);
+  P.im.assign((size_t)K * K, 0.0);
+  for (int a = 0; a < K; a++) P.re[(size_t)a * K + a] = 1.0;
   auto bit_of = [&](int q) {
     for (int j = 0; j < k; j++)
       if (item.qubits[j] == q) return j;
     return -1;
   };
+  int touched = 0;
   for (int g : item.gates) {
     const qcs_cuda_op &o = ops[g];
     double m[8];
     gate_matrix(o.kind, o.angle, m);
-    cd g00(m[0], m[1]), g01(m[2], m[3]), g10(m[4], m[5]), g11(m[6], m[7]);
-    int tb = 1 << bit_of(o.target);
-    int cb = gate_is_controlled(o.kind) ? (1 << bit_of(o.control)) : 0;
-    // U := G * U, i.e. apply the gate to every column of U
-    for (int a = 0; a < K; a++) {
-      if (a & tb) continue;
-      if (cb && !(a & cb)) continue;
-      cd *r0 = &u[(size_t)a * K];
-      cd *r1 = &u[(size_t)(a | tb) * K];
-      for (int col = 0; col < K; col++) {
-        cd v0 = r0[col], v1 = r1[col];
-        r0[col] = g00 * v0 + g01 * v1;
-        r1[col] = g10 * v0 + g11 * v1;
-      }
-    }
+    const int tb = 1 << bit_of(o.target);
+    const int cb = gate_is_controlled(o.kind) ? (1 << bit_of(o.control)) : 0;
+    touched |= tb | cb;
+    apply_gate_planes(P, m, tb, cb, touched);
   }
+  u.resize((size_t)K * K);
+  for (size_t i = 0; i < (size_t)K * K; i++) u[i] = cd(P.re[i], P.im[i]);
 }
 
 }  // namespace qcs

@@ -2,13 +2,11 @@
 //
 // Who needs it: callers that cannot call cudaMalloc on the path where they
 // sample.  Examples are a host application that owns all device memory
-// through its own pool and forbids libraries from allocating, code that must
-// not take cudaMalloc's implicit device synchronisation (latency-critical
-// serving loops), and code that prepares work while a CUDA stream is being
-// captured into a graph, where allocation calls are not part of the captured
-// work.  qcs_cuda_sample keeps its scratch in per-state buffers it allocates
-// on first use; this variant keeps it in one fixed array that is part of the
-// library image instead.
+// through its own pool and forbids libraries from allocating, and code that
+// must not take cudaMalloc's implicit device synchronisation (latency-
+// critical serving loops).  qcs_cuda_sample keeps its scratch in per-state
+// buffers it allocates on first use; this variant keeps it in one fixed
+// array that is part of the library image instead.
 //
 // The scratch is the per-tile probability prefix of the sampler: one double
 // per tile of 4096 amplitudes plus the total.  It lives in a file-scope
@@ -19,7 +17,9 @@
 // Host code cannot use the array's name as a device address, so the device
 // address is looked up with cudaGetSymbolAddress once per device, with that
 // device current, on the first call made on it.  That first call should come
-// before any stream capture that the caller starts.
+// before any stream capture that the caller starts.  A device reset
+// (cudaDeviceReset) ends the context the address belongs to; a call whose
+// launch fails forgets the address, so the next call looks it up again.
 //
 // Every call writes every prefix entry it later reads, so no entry has to
 // start at zero; the array simply keeps the previous call's values.  All
@@ -175,17 +175,28 @@ __global__ void k_na_sample(const C *v, i64 tile, i64 n_tiles, const double *pre
   }
 }
 
+// Forgets the current device's scratch address (after a failed launch).
+static void noalloc_forget() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  g_noalloc_addr[dev] = nullptr;
+}
+
 template <typename C>
 static int na_launch(const C *v, i64 count, const double *draws, int shots, i64 *samples,
                      cudaStream_t st, double *prefix) {
   const i64 tile = count < kNoAllocTile ? count : kNoAllocTile;
   const i64 n_tiles = count / tile;
   int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (!rc)
+    rc = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                    "cudaDeviceGetAttribute(multiprocessor count)");
+  if (rc) return rc;
   const int gt = (int)(n_tiles < (i64)sms * 8 ? n_tiles : (i64)sms * 8);
   k_na_tile_sums<C><<<gt, 256, 0, st>>>(v, tile, n_tiles, prefix);
-  int rc = check_launch("sample_noalloc tile sums");
+  rc = check_launch("sample_noalloc tile sums");
   if (rc) return rc;
   k_na_prefix<<<1, 1024, 0, st>>>(prefix, n_tiles);
   rc = check_launch("sample_noalloc prefix");
@@ -220,8 +231,11 @@ extern "C" int qcs_cuda_sample_noalloc(const void *amplitudes, long long count, 
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == QCS_CUDA_C128)
-    return na_launch<double2>((const double2 *)amplitudes, count, draws, shots, (i64 *)samples,
-                              st, prefix);
-  return na_launch<float2>((const float2 *)amplitudes, count, draws, shots, (i64 *)samples, st,
+    rc = na_launch<double2>((const double2 *)amplitudes, count, draws, shots, (i64 *)samples,
+                            st, prefix);
+  else
+    rc = na_launch<float2>((const float2 *)amplitudes, count, draws, shots, (i64 *)samples, st,
                            prefix);
+  if (rc == QCS_CUDA_ELAUNCH) noalloc_forget();
+  return rc;
 }

@@ -5,11 +5,15 @@
   rank (no data-path collective);
 * the reference arm runs on rank 0 only; other ranks return without work;
 * a rank that raises leaves the other rank's collective with an error
-  instead of a hang (short process-group timeout).
+  instead of a hang (short process-group timeout);
+* `bench.py --gpus 2` started without a launcher starts its two ranks itself
+  (torch.distributed.run on 127.0.0.1), and rank 0 prints one line for both.
 """
 import json
 import os
 import socket
+import subprocess
+import sys
 
 import pytest
 import torch.multiprocessing as mp
@@ -87,3 +91,22 @@ def test_a_failed_rank_ends_the_other_ranks_collective_with_an_error(tmp_path):
     res = _spawn(tmp_path, "fail")
     assert len(res) == 1 and res[0]["rank"] == 0
     assert res[0]["error"] is not None
+
+
+def test_bench_gpus_2_starts_two_ranks():
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT")}
+    p = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2",
+                        "--workload", "shards", "--instances", "37"],
+                       capture_output=True, text=True, timeout=300, env=env, cwd=root)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, p.stdout[-2000:]  # rank 0 alone prints
+    out = json.loads(lines[0])
+    assert out["n_gpus"] == 2
+    ranks = out["ranks"]
+    assert [r["rank"] for r in ranks] == [0, 1]
+    assert ranks[0]["pid"] != ranks[1]["pid"]  # two processes ran
+    a, b = set(ranks[0]["instances"]), set(ranks[1]["instances"])
+    assert not (a & b) and a | b == set(range(37))

@@ -1,9 +1,9 @@
 """The allocation-free sampler, qcs_cuda_sample_noalloc, through the C ABI.
 
 Some callers cannot let a library call cudaMalloc where they sample: a host
-application that hands out all device memory from its own pool, a
+application that hands out all device memory from its own pool, or a
 latency-critical loop that must not take cudaMalloc's implicit device
-synchronisation, or code that prepares work while a stream is captured.  For
+synchronisation.  For
 them the sampler keeps its scratch in a fixed array inside the library, and
 the caller passes the amplitudes, the draws and the output as device
 pointers.  It must give the same indices as qcs_cuda_sample, which keeps its
@@ -49,6 +49,26 @@ def test_sample_noalloc_matches_sample_two_calls_in_a_row():
         # identical rule and arithmetic: the indices must agree exactly
         assert np.array_equal(got, want), (n, int(np.sum(got != want)))
         assert np.all(got >= 0)
+
+
+def test_sample_noalloc_matches_sample_on_states_below_one_warp():
+    """States of 2, 8 and 32 amplitudes (one tile narrower than a warp), and
+    a call with no shots, which only refreshes the scratch."""
+    torch = pytest.importorskip("torch")
+    for n, prec in ((1, capi.C64), (3, capi.C128), (5, capi.C64)):
+        g = W.one_qubit_circuit(n, n, 12)
+        draws = np.random.default_rng(n).random(257)
+        with capi.State(n, prec) as s:
+            s.run(g)
+            want = s.sample(draws)
+            got = _noalloc(s, draws, torch)
+            assert np.array_equal(got, want), (n, got[got != want][:5])
+            rc = capi.lib().qcs_cuda_sample_noalloc(
+                C.c_void_p(s.device_ptr()), s.size, s.precision, None, 0, None,
+                C.c_void_p(s.stream()))
+            assert rc == capi.OK, capi.lib().qcs_cuda_last_error()
+            s.synchronize()
+            assert np.array_equal(_noalloc(s, draws, torch), want)
 
 
 def test_sample_noalloc_rejects_sizes_beyond_its_scratch():
