@@ -567,7 +567,13 @@ def run_sweeps(args, dist):
             "measure": (lambda i: s.measure(i % n, 0.5), 2.5 * Ns),
             "sample": (lambda i: s.sample(draws), Ns),
         }
+        us = {5: u5, 6: u6, 7: u7}
         for name in only:
+            # block_tc<k>_at<q>: a k-qubit tensor-core block on qubits q..q+k-1
+            if name not in ops and name.startswith("block_tc") and "_at" in name:
+                kk, q0 = int(name[8]), int(name.split("_at")[1])
+                ops[name] = ((lambda i, q=list(range(q0, q0 + kk)), u=us[kk]:
+                              s.apply_block(q, u, capi.FUSE_TENSOR)), 2 * Ns)
             fn, nbytes = ops[name]
             for i in range(args.warmup):
                 fn(i)
