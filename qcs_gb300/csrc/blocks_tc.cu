@@ -150,62 +150,8 @@ struct Tc7 {
   static_assert(UPT == 1 && CHUNKS % 2 == 0, "producer shares and stage pairs");
 };
 
-// k = 7 with the block matrix in tensor memory (k_block_tc7t).  The product
-// is computed transposed, D^T[o][m] = sum_i U[o][i] X[m][i]: A = U (M = 128
-// outputs = TMEM lanes, K = 128 inputs) is read by the tensor cores straight
-// from TMEM, B = a chunk of the state tile (N = 64 columns x K = 32
-// amplitudes) from shared memory.  Against Tc7, where both operands come
-// from shared memory, each MMA reads half the shared-memory bytes, and the
-// 128 KB the matrix took there hold eight operand stages instead of two.
-// TMEM: the four U operands (Re hi, Re lo, Im hi, Im lo) take 4 x 64
-// columns (128 bf16 a lane); the accumulators Re and Im of a 64-column tile
-// take 2 x 64, double buffered.  The epilogue thread of TMEM lane o owns
-// output amplitude o of every column of the tile.
-struct Tc7T {
-  static constexpr int KA = 128;                  // amplitudes per column = UMMA M
-  static constexpr int TN = 64;                   // state columns per tile = UMMA N
-  static constexpr int COL_BITS = 6;              // column qubits per tile
-  static constexpr int KC = 32;                   // amplitudes per K-chunk
-  static constexpr int CHUNKS = KA / KC;          // per tile
-  static constexpr int STAGES = 8;                // operand stages in shared memory
-  static constexpr int OP_BYTES = TN * KC * 2;    // one bf16 chunk operand (64-byte swizzle)
-  static constexpr int STAGE_BYTES = 4 * OP_BYTES;  // Xr hi, Xr lo, Xi hi, Xi lo
-  static constexpr int PROD_WARPS = 16;
-  static constexpr int PROD_THREADS = 32 * PROD_WARPS;
-  static constexpr int MMA_WARP = kTcEpiWarps + PROD_WARPS;
-  static constexpr int THREADS = 32 * (MMA_WARP + 1);
-  static constexpr int UNIT = 4;                  // amplitudes a producer converts per chunk
-  static constexpr int SQ_PARTS = KC / UNIT;      // producers per column of a chunk
-  static constexpr int AHEAD = 4;                 // chunks a producer holds in registers
-  // Norm slot s is refilled for tile it + SQ_SLOTS; the producers can be
-  // STAGES / CHUNKS tiles ahead of the MMAs, which are one accumulator
-  // stage ahead of the epilogue.
-  static constexpr int SQ_SLOTS = STAGES / CHUNKS + 2;
-  static constexpr int U_COLS = KA / 2;           // TMEM columns of one U operand
-  static constexpr int ACC0 = 4 * U_COLS;         // first accumulator column
-  static constexpr int TMEM_COLS = 512;
-  static constexpr int U_BYTES = KA * KA * 2;     // one U operand in the image
-  static constexpr int IMG_BYTES = 4 * U_BYTES;
-  static constexpr int NBARS = 2 * STAGES + 5 + SQ_SLOTS;
-  static constexpr int OFF_A = 0;                 // [stage][operand][OP_BYTES]
-  static constexpr int OFF_COL = OFF_A + STAGES * STAGE_BYTES;
-  static constexpr int OFF_BLK = OFF_COL + TN * 8;
-  static constexpr int OFF_SQ = OFF_BLK + KA * 8;   // float [slot][part][column]
-  static constexpr int OFF_RED = OFF_SQ + SQ_SLOTS * SQ_PARTS * TN * 4;  // float [warp][column]
-  static constexpr int OFF_SCALE = OFF_RED + kTcEpiWarps * TN * 4;       // float [column]
-  static constexpr int OFF_BAR = OFF_SCALE + TN * 4;
-  static constexpr int OFF_MISC = OFF_BAR + NBARS * 8;
-  static constexpr int SMEM = OFF_MISC + 16 + 1024;
-  static_assert(SMEM <= 232448, "exceeds the 227 KB shared-memory opt-in");
-  static_assert(TN * KC / UNIT == PROD_THREADS, "one unit per producer thread and chunk");
-  static_assert(ACC0 + 2 * 2 * TN == TMEM_COLS, "TMEM budget");
-  static_assert(STAGES % CHUNKS == 0 && (CHUNKS % AHEAD == 0 || AHEAD % CHUNKS == 0),
-                "stage and register rings");
-};
-
 // An upload slot: the largest (k = 7) image, then the block's row sums (float2).
 constexpr size_t kImgSlotBytes = Tc7::IMG_BYTES + Tc7::KA * 8;
-static_assert(Tc7T::IMG_BYTES == Tc7::IMG_BYTES, "both k = 7 images fit a slot");
 
 struct TcGeom {
   i64 n_tiles;
@@ -1065,397 +1011,6 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
   }
 }
 
-// k = 7 with the block matrix in tensor memory (Tc7T).  Roles as in
-// k_block_tc7 (4 epilogue warps, 16 producer warps, 1 MMA warp), with these
-// differences:
-//   set-up     the epilogue warps store U into TMEM (thread o: row o of the
-//              four operands, tcgen05.st);
-//   producers  one 4-amplitude unit of a 64-column x 32-amplitude chunk
-//              each, four chunks (one tile) held in registers ahead of their
-//              conversion, eight shared-memory stages;
-//   MMA        12 products per 16-amplitude K-step (M = 128 outputs, N = 64
-//              columns), A from TMEM;
-//   epilogue   thread o holds output o of the tile's 64 columns: the column
-//              norms of the result are summed across lanes by a butterfly
-//              (fixed order) and across the four warps through shared
-//              memory, and each store instruction writes one output of 32
-//              columns (kLowMode: 32 adjacent amplitudes).
-// Every decision to leave the epilogue loop is taken by all four epilogue
-// warps together (bar.red.and), so the named barriers inside a tile are
-// always reached by all 128 threads.
-template <int MODE, bool FUSED>
-__global__ void __launch_bounds__(Tc7T::THREADS, 1)
-    k_block_tc7t(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
-                 const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err) {
-  using S = Tc7T;
-  extern __shared__ uint8_t smem_dyn[];
-  const uint32_t raw = smem_u32(smem_dyn);
-  uint8_t *smem = smem_dyn + ((1024u - (raw & 1023u)) & 1023u);
-  uint8_t *sA = smem + S::OFF_A;
-  i64 *col_off = reinterpret_cast<i64 *>(smem + S::OFF_COL);
-  i64 *blk_off = reinterpret_cast<i64 *>(smem + S::OFF_BLK);
-  float *colsq = reinterpret_cast<float *>(smem + S::OFF_SQ);
-  float *red = reinterpret_cast<float *>(smem + S::OFF_RED);
-  float *scl = reinterpret_cast<float *>(smem + S::OFF_SCALE);
-  const uint32_t bar0 = smem_u32(smem + S::OFF_BAR);
-  // 8-byte barriers: full[stage], free[stage], acc_full[2], acc_empty[2],
-  // drain, sq_full[slot] (a tile's column norms are in colsq[slot])
-  constexpr int FULL = 0, FREE = S::STAGES, ACCF = 2 * S::STAGES, ACCE = ACCF + 2,
-                DRAIN = ACCE + 2, SQF = DRAIN + 1;
-  auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::OFF_MISC);
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::OFF_MISC + 4);
-
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-
-  if (tid == 0) {
-    for (int i = 0; i < S::STAGES; i++) {
-      mbar_init(bar(FULL + i), S::PROD_THREADS);
-      mbar_init(bar(FREE + i), 1);
-    }
-    mbar_init(bar(ACCF), 1);
-    mbar_init(bar(ACCF + 1), 1);
-    mbar_init(bar(ACCE), kTcEpiThreads);
-    mbar_init(bar(ACCE + 1), kTcEpiThreads);
-    mbar_init(bar(DRAIN), 1);
-    for (int k = 0; k < S::SQ_SLOTS; k++) mbar_init(bar(SQF + k), S::PROD_THREADS);
-    *abort_flag = 0;
-    fence_barrier_init();
-  }
-  for (int i = tid; i < S::TN; i += S::THREADS) col_off[i] = g.col_off[i];
-  for (int i = tid; i < S::KA; i += S::THREADS) blk_off[i] = g.blk_off[i];
-  if (warp == S::MMA_WARP) {
-    tmem_alloc(smem_u32(tmem_slot), S::TMEM_COLS);
-    tmem_relinquish();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-  // U into TMEM: epilogue warp w owns TMEM lanes 32w .. 32w+31, thread o
-  // stores row o of each operand (128 bf16 = 64 columns)
-  float2 beta_o = make_float2(0.f, 0.f);
-  if (warp < kTcEpiWarps) {
-    const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
-#pragma unroll 1
-    for (int op = 0; op < 4; op++) {
-      const uint4 *row = bimg + ((size_t)op * S::KA + tid) * (S::KA * 2 / 16);
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        uint32_t r[16];
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const uint4 t = row[4 * j + i];
-          r[4 * i] = t.x;
-          r[4 * i + 1] = t.y;
-          r[4 * i + 2] = t.z;
-          r[4 * i + 3] = t.w;
-        }
-        tmem_st16(tmem + lane_addr + (uint32_t)(op * S::U_COLS + 16 * j), r);
-      }
-    }
-    tmem_wait_st();
-    if (FUSED && diffuse_sum) {  // beta[o] = 2m * (row sum o of U), as in k_block_tc
-      const float tr = (float)(2.0 * (diffuse_sum[0] * inv_n));
-      const float ti = (float)(2.0 * (diffuse_sum[1] * inv_n));
-      const float2 r = reinterpret_cast<const float2 *>(bimg + S::IMG_BYTES / 16)[tid];
-      beta_o = make_float2(tr * r.x - ti * r.y, tr * r.y + ti * r.x);
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-
-  if (warp >= kTcEpiWarps && warp < S::MMA_WARP) {
-    // ---------------- producers ----------------
-    // kColMode / kPairMode: thread p converts column p % 64, amplitudes
-    // 4u .. 4u+3 of each chunk, u = p / 64 (a warp: 32 adjacent columns);
-    // kLowMode: column p / 8, amplitudes 2u, 2u+1, 16+2u, 17+2u, u = p % 8
-    // (a warp instruction: 4 columns x 128 contiguous bytes).  Chunk c of
-    // tile it is held in register set c from the conversion of chunk c of
-    // tile it - 1 until its own.  Stage reuse: chunk q goes to stage
-    // q % STAGES once the MMAs of chunk q - STAGES are done.  Norm slot
-    // it % SQ_SLOTS: when tile it's last chunk is converted, the MMAs of
-    // tile it - 2 have been issued, which waited for the epilogue of tile
-    // it - 4, the slot's last reader.
-    const int p = tid - kTcEpiThreads;
-    const int m = MODE == kLowMode ? (p >> 3) : (p & (S::TN - 1));
-    const int u = MODE == kLowMode ? (p & 7) : (p >> 6);
-    float2 x[S::CHUNKS][S::UNIT];
-    const TileWalk w = tile_walk(g);
-    auto load = [&](auto cc, i64 base) {
-      constexpr int c = decltype(cc)::value;
-      const float2 *src = v + base + col_off[m];
-      if constexpr (MODE == kLowMode) {
-        const float4 a = *reinterpret_cast<const float4 *>(src + c * S::KC + 2 * u);
-        const float4 b = *reinterpret_cast<const float4 *>(src + c * S::KC + 16 + 2 * u);
-        x[c][0] = make_float2(a.x, a.y);
-        x[c][1] = make_float2(a.z, a.w);
-        x[c][2] = make_float2(b.x, b.y);
-        x[c][3] = make_float2(b.z, b.w);
-      } else if constexpr (MODE == kPairMode) {
-        const int a0 = c * S::KC + S::UNIT * u;
-        const float4 a = *reinterpret_cast<const float4 *>(src + blk_off[a0]);
-        const float4 b = *reinterpret_cast<const float4 *>(src + blk_off[a0 + 2]);
-        x[c][0] = make_float2(a.x, a.y);
-        x[c][1] = make_float2(a.z, a.w);
-        x[c][2] = make_float2(b.x, b.y);
-        x[c][3] = make_float2(b.z, b.w);
-      } else {
-        const int a0 = c * S::KC + S::UNIT * u;
-#pragma unroll
-        for (int e = 0; e < S::UNIT; e++) x[c][e] = src[blk_off[a0 + e]];
-      }
-    };
-    // hi and lo of two amplitudes' real and imaginary parts
-    auto split2 = [&](float2 x0, float2 x1, uint32_t *wd) {
-      const __nv_bfloat162 rh = __floats2bfloat162_rn(x0.x, x1.x);
-      const __nv_bfloat162 ih = __floats2bfloat162_rn(x0.y, x1.y);
-      const float2 rf = __bfloat1622float2(rh), imf = __bfloat1622float2(ih);
-      const __nv_bfloat162 rl = __floats2bfloat162_rn(x0.x - rf.x, x1.x - rf.y);
-      const __nv_bfloat162 il = __floats2bfloat162_rn(x0.y - imf.x, x1.y - imf.y);
-      wd[0] = *reinterpret_cast<const uint32_t *>(&rh);
-      wd[1] = *reinterpret_cast<const uint32_t *>(&rl);
-      wd[2] = *reinterpret_cast<const uint32_t *>(&ih);
-      wd[3] = *reinterpret_cast<const uint32_t *>(&il);
-      return x0.x * x0.x + x0.y * x0.y + x1.x * x1.x + x1.y * x1.y;
-    };
-    float part = 0.f;
-    auto convert = [&](auto cc, int st) {
-      constexpr int c = decltype(cc)::value;
-      uint8_t *sb = sA + st * S::STAGE_BYTES;
-      uint32_t w0[4], w1[4];
-      part += split2(x[c][0], x[c][1], w0);
-      part += split2(x[c][2], x[c][3], w1);
-      if constexpr (MODE == kLowMode) {
-        const int off0 = sw64_offset(m, 2 * u), off1 = sw64_offset(m, 16 + 2 * u);
-#pragma unroll
-        for (int o = 0; o < 4; o++) {
-          *reinterpret_cast<uint32_t *>(sb + o * S::OP_BYTES + off0) = w0[o];
-          *reinterpret_cast<uint32_t *>(sb + o * S::OP_BYTES + off1) = w1[o];
-        }
-      } else {
-        const int off = sw64_offset(m, S::UNIT * u);
-#pragma unroll
-        for (int o = 0; o < 4; o++)
-          *reinterpret_cast<uint2 *>(sb + o * S::OP_BYTES + off) = make_uint2(w0[o], w1[o]);
-      }
-    };
-    i64 nbase = 0;
-    // chunk c of tile it: false when the CTA is aborting
-    auto step = [&](auto cc, i64 it) -> bool {
-      constexpr int c = decltype(cc)::value;
-      const i64 q = it * S::CHUNKS + c;
-      const int st = (int)(q % S::STAGES);
-      if (c == 0) {
-        if (p < g.nruns && it + g.pf_ahead < w.count)
-          prefetch_l2(v + tile_base(w.at(it + g.pf_ahead), g) + g.run_off[p],
-                      (uint32_t)g.run_bytes);
-        nbase = it + 1 < w.count ? tile_base(w.at(it + 1), g) : 0;
-        part = 0.f;
-      }
-      if (q >= S::STAGES &&
-          !wait_bar(bar(FREE + st), (uint32_t)((q / S::STAGES - 1) & 1), abort_flag, err, 1))
-        return false;
-      convert(cc, st);
-      if (it + 1 < w.count) load(cc, nbase);
-      if (c == S::CHUNKS - 1) colsq[((int)(it % S::SQ_SLOTS) * S::SQ_PARTS + u) * S::TN + m] = part;
-      fence_async_shared();
-      mbar_arrive(bar(FULL + st));
-      if (c == S::CHUNKS - 1) mbar_arrive(bar(SQF + (int)(it % S::SQ_SLOTS)));
-      return true;
-    };
-    const std::integral_constant<int, 0> c0{};
-    const std::integral_constant<int, 1> c1{};
-    const std::integral_constant<int, 2> c2{};
-    const std::integral_constant<int, 3> c3{};
-    static_assert(S::CHUNKS == 4 && S::AHEAD == S::CHUNKS, "one tile of chunks in registers");
-    if (w.count > 0) {
-      const i64 b0 = tile_base(w.at(0), g);
-      load(c0, b0);
-      load(c1, b0);
-      load(c2, b0);
-      load(c3, b0);
-    }
-    for (i64 it = 0; it < w.count; ++it)
-      if (!step(c0, it) || !step(c1, it) || !step(c2, it) || !step(c3, it)) break;
-  } else if (warp == S::MMA_WARP) {
-    // ---------------- MMA issue ----------------
-    if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16(S::KA, S::TN);
-      constexpr uint32_t idesc_neg = idesc | (1u << 14);  // negate B
-      const uint32_t a0 = smem_u32(sA);
-      const uint32_t urh = tmem, url = tmem + S::U_COLS, uih = tmem + 2 * S::U_COLS,
-                     uil = tmem + 3 * S::U_COLS;
-      const TileWalk w = tile_walk(g);
-      bool ok = true;
-      for (i64 it = 0; ok && it < w.count; ++it) {
-        const int acc = (int)(it & 1);
-        if (it >= 2 &&
-            !wait_bar(bar(ACCE + acc), (uint32_t)(((it - 2) >> 1) & 1), abort_flag, err, 3))
-          break;
-        const uint32_t dre = tmem + (uint32_t)(S::ACC0 + acc * 2 * S::TN), dim = dre + S::TN;
-        for (int c = 0; c < S::CHUNKS; c++) {
-          const i64 q = it * S::CHUNKS + c;
-          const int st = (int)(q % S::STAGES);
-          if (!wait_bar(bar(FULL + st), (uint32_t)((q / S::STAGES) & 1), abort_flag, err, 2)) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          const uint32_t sb = a0 + (uint32_t)(st * S::STAGE_BYTES);
-#pragma unroll
-          for (int s = 0; s < S::KC / 16; s++) {
-            const uint32_t kk = (uint32_t)((c * S::KC + 16 * s) / 2);  // TMEM column of U
-            const uint32_t ka = (uint32_t)(s * 32);
-            const uint64_t xrh = sw64_desc(sb + 0 * S::OP_BYTES + ka);
-            const uint64_t xrl = sw64_desc(sb + 1 * S::OP_BYTES + ka);
-            const uint64_t xih = sw64_desc(sb + 2 * S::OP_BYTES + ka);
-            const uint64_t xil = sw64_desc(sb + 3 * S::OP_BYTES + ka);
-            const uint32_t first = (c > 0 || s > 0) ? 1u : 0u;
-            umma_bf16_ta(dre, urh + kk, xrh, idesc, first);  // Re += Ur Xr
-            umma_bf16_ta(dre, urh + kk, xrl, idesc, 1u);
-            umma_bf16_ta(dre, url + kk, xrh, idesc, 1u);
-            umma_bf16_ta(dre, uih + kk, xih, idesc_neg, 1u);  // Re -= Ui Xi
-            umma_bf16_ta(dre, uih + kk, xil, idesc_neg, 1u);
-            umma_bf16_ta(dre, uil + kk, xih, idesc_neg, 1u);
-            umma_bf16_ta(dim, uih + kk, xrh, idesc, first);  // Im += Ui Xr
-            umma_bf16_ta(dim, uih + kk, xrl, idesc, 1u);
-            umma_bf16_ta(dim, uil + kk, xrh, idesc, 1u);
-            umma_bf16_ta(dim, urh + kk, xih, idesc, 1u);  // Im += Ur Xi
-            umma_bf16_ta(dim, urh + kk, xil, idesc, 1u);
-            umma_bf16_ta(dim, url + kk, xih, idesc, 1u);
-          }
-          umma_commit(bar(FREE + st));
-        }
-        if (ok) umma_commit(bar(ACCF + acc));
-      }
-      umma_commit(bar(DRAIN));
-      long long t0 = clock64();
-      while (!mbar_try_wait(bar(DRAIN), 0)) {
-        if (clock64() - t0 > kWaitCycles) {
-          atomicExch(err, 4);
-          break;
-        }
-      }
-    }
-    __syncwarp();
-  } else {
-    // ---------------- epilogue ----------------
-    const int o = tid;  // TMEM lane = output amplitude of the block
-    const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
-    const TileWalk w = tile_walk(g);
-    // after the reduce-scatter below, lanes 2c and 2c + 1 hold column c's sum
-    const int bcol = lane >> 1;
-    double sum_re = 0.0, sum_im = 0.0;
-    for (i64 it = 0; it < w.count; ++it) {
-      const int acc = (int)(it & 1);
-      const int slot = (int)(it % S::SQ_SLOTS);
-      bool ok = wait_bar(bar(ACCF + acc), (uint32_t)((it >> 1) & 1), abort_flag, err, 5);
-      ok = ok && wait_bar(bar(SQF + slot), (uint32_t)((it / S::SQ_SLOTS) & 1), abort_flag, err, 6);
-      if (!bar_and(1, kTcEpiThreads, ok)) break;
-      tc_fence_after();
-      const uint32_t tre = tmem + lane_addr + (uint32_t)(S::ACC0 + acc * 2 * S::TN);
-      const uint32_t tim = tre + (uint32_t)S::TN;
-      if (renorm) {
-#pragma unroll 1
-        for (int gq = 0; gq < S::TN / 16; gq++) {
-          float re[16], im[16];
-          tmem_ld16x2(tre + 16 * gq, tim + 16 * gq, re, im);
-          float xs[16];
-#pragma unroll
-          for (int j = 0; j < 16; j++) xs[j] = re[j] * re[j] + im[j] * im[j];
-          // reduce-scatter of 16 column sums over the 32 lanes (fixed order)
-#pragma unroll
-          for (int st = 0; st < 4; st++) {
-            const int off = 16 >> st, half = 8 >> st;
-            const bool up = (lane & off) != 0;
-#pragma unroll
-            for (int j = 0; j < half; j++) {
-              const float send = up ? xs[j] : xs[half + j];
-              const float keep = up ? xs[half + j] : xs[j];
-              xs[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
-            }
-          }
-          xs[0] += __shfl_xor_sync(0xffffffffu, xs[0], 1);
-          if ((lane & 1) == 0) red[warp * S::TN + 16 * gq + bcol] = xs[0];
-        }
-        bar_sync_n(1, kTcEpiThreads);
-        if (tid < S::TN) {
-          const float out = ((red[tid] + red[S::TN + tid]) + red[2 * S::TN + tid]) +
-                            red[3 * S::TN + tid];
-          const float *sq = colsq + slot * S::SQ_PARTS * S::TN;
-          float in = 0.f;
-#pragma unroll
-          for (int h = 0; h < S::SQ_PARTS; h++) in += sq[h * S::TN + tid];
-          scl[tid] = out > 0.f ? sqrtf(in / out) : 1.f;
-        }
-        bar_sync_n(1, kTcEpiThreads);
-      }
-      float2 *dst = v + tile_base(w.at(it), g) + blk_off[o];
-#pragma unroll 1
-      for (int gq = 0; gq < S::TN / 16; gq++) {
-        float re[16], im[16];
-        tmem_ld16x2(tre + 16 * gq, tim + 16 * gq, re, im);
-        float pr = 0.f, pi = 0.f;
-#pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const float sc = renorm ? scl[16 * gq + j] : 1.f;
-          re[j] *= sc;
-          im[j] *= sc;
-          if constexpr (FUSED) {
-            if (diffuse_sum) {
-              re[j] = beta_o.x - re[j];
-              im[j] = beta_o.y - im[j];
-            }
-            pr += re[j];
-            pi += im[j];
-          }
-        }
-        if constexpr (FUSED) {
-          if (sum_out) {
-            sum_re += (double)pr;
-            sum_im += (double)pi;
-          }
-        }
-        if constexpr (MODE == kColMode) {  // columns 2j, 2j+1 are adjacent amplitudes
-#pragma unroll
-          for (int j = 0; j < 16; j += 2)
-            *reinterpret_cast<float4 *>(dst + col_off[16 * gq + j]) =
-                make_float4(re[j], im[j], re[j + 1], im[j + 1]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; j++) dst[col_off[16 * gq + j]] = make_float2(re[j], im[j]);
-        }
-      }
-      tc_fence_before();
-      mbar_arrive(bar(ACCE + acc));
-    }
-    if (FUSED && sum_out) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        sum_re += __shfl_xor_sync(0xffffffffu, sum_re, off);
-        sum_im += __shfl_xor_sync(0xffffffffu, sum_im, off);
-      }
-      if (lane == 0) {
-        ReduceSlot r;
-        r.a = sum_re;
-        r.b = sum_im;
-        r.c = 0.0;
-        r.d = 0.0;
-        sum_out[blockIdx.x * kTcEpiWarps + warp] = r;
-      }
-    }
-  }
-
-  tc_fence_before();
-  __syncthreads();
-  if (warp == S::MMA_WARP) {
-    tc_fence_after();
-    tmem_dealloc(tmem, S::TMEM_COLS);
-  }
-}
-
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -1551,43 +1106,6 @@ static int launch_tc7(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int 
   return launched(s, KC_BLOCK_TC7, 2.0 * s->size * 8.0, "apply_block (tcgen05, k = 7)");
 }
 
-// 7-qubit blocks run with the matrix in tensor memory (k_block_tc7t) unless
-// QCS_TC7=smem selects the kernel that keeps it in shared memory
-// (k_block_tc7).  Read once per process.
-static bool tc7_in_tmem() {
-  static const bool t = [] {
-    const char *e = getenv("QCS_TC7");
-    return !(e && strcmp(e, "smem") == 0);
-  }();
-  return t;
-}
-
-template <int MODE>
-static int launch_tc7t(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int renorm,
-                       const double *diffuse_sum, ReduceSlot *sum_out) {
-  static bool configured = false;
-  if (!configured) {
-    int rc = check_cuda(cudaFuncSetAttribute(k_block_tc7t<MODE, false>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Tc7T::SMEM),
-                        "cudaFuncSetAttribute(tcgen05 block, k = 7, matrix in TMEM)");
-    if (!rc)
-      rc = check_cuda(cudaFuncSetAttribute(k_block_tc7t<MODE, true>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, Tc7T::SMEM),
-                      "cudaFuncSetAttribute(tcgen05 block, k = 7, matrix in TMEM, fused)");
-    if (rc) return rc;
-    configured = true;
-  }
-  const int grid = (int)(g.n_tiles < (i64)s->dev.num_sms ? g.n_tiles : s->dev.num_sms);
-  prof_begin(s);
-  if (diffuse_sum || sum_out)
-    k_block_tc7t<MODE, true><<<grid, Tc7T::THREADS, Tc7T::SMEM, s->stream>>>(
-        (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err);
-  else
-    k_block_tc7t<MODE, false><<<grid, Tc7T::THREADS, Tc7T::SMEM, s->stream>>>(
-        (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err);
-  return launched(s, KC_BLOCK_TC7, 2.0 * s->size * 8.0, "apply_block (tcgen05, k = 7, matrix in TMEM)");
-}
-
 // Whether U is unitary (to FP64 rounding): unitary blocks get the
 // per-column norm restore.  Checked as |U^H U v - v| <= 1e-9 |v| for two
 // fixed pseudo-random vectors v, O(K^2) instead of the O(K^3) of forming
@@ -1636,7 +1154,6 @@ static bool is_unitary(const double *u, int K) {
 // fused diffusion needs.
 struct TcResident {
   int k = 0, mode = 0, renorm = 0;
-  bool t7 = false;  // k = 7 with the matrix in tensor memory (k_block_tc7t)
   size_t image_bytes = 0;
   TcGeom g;
   std::vector<uint8_t> image;  // host copy
@@ -1680,12 +1197,8 @@ static void tc_prepare(const qcs_cuda_state *s, int k, const int *qubits_in, con
   memset(&g, 0, sizeof(g));
   std::vector<int> role(s->n, -1);  // >= 0 block bit, -2 column, -1 free
   for (int j = 0; j < k; j++) role[qubits[j]] = j;
-  // k = 7 with the matrix in tensor memory tiles 64 columns (6 column
-  // qubits); every other layout 128
-  const bool t7 = k == 7 && tc7_in_tmem();
-  const int ncol = t7 ? Tc7T::COL_BITS : 7;
   std::vector<int> colq;
-  for (int q = 0; q < s->n && (int)colq.size() < ncol; q++)
+  for (int q = 0; q < s->n && (int)colq.size() < 7; q++)
     if (role[q] == -1) {
       role[q] = -2;
       colq.push_back(q);
@@ -1700,9 +1213,9 @@ static void tc_prepare(const qcs_cuda_state *s, int k, const int *qubits_in, con
       g.nib[k][v] = o;
     }
   g.n_tiles = 1LL << g.nfree;
-  for (int m = 0; m < (1 << ncol); m++) {
+  for (int m = 0; m < kTcM; m++) {
     i64 o = 0;
-    for (int b = 0; b < ncol; b++)
+    for (int b = 0; b < 7; b++)
       if ((m >> b) & 1) o |= 1LL << colq[b];
     g.col_off[m] = o;
   }
@@ -1713,8 +1226,8 @@ static void tc_prepare(const qcs_cuda_state *s, int k, const int *qubits_in, con
     g.blk_off[a] = o;
   }
   {
-    // the tile's qubits ascending; the lowest R of them are 0..R-1 (R >=
-    // ncol), so the tile is 2^(k+ncol-R) runs of 2^R adjacent amplitudes
+    // the tile's qubits ascending; the lowest R of them are 0..R-1 (R >= 7),
+    // so the tile is 2^(k+7-R) runs of 2^R adjacent amplitudes
     std::vector<int> tq;
     for (int q = 0; q < s->n; q++)
       if (role[q] != -1) tq.push_back(q);
@@ -1735,12 +1248,11 @@ static void tc_prepare(const qcs_cuda_state *s, int k, const int *qubits_in, con
         if ((run >> (b - R)) & 1) o |= 1LL << tq[b];
       g.run_off[j] = o;
     }
-    g.pf_ahead = t7 ? 2 : pf_ahead(k);
+    g.pf_ahead = pf_ahead(k);
   }
   bool low = true;  // the block is exactly qubits 0..k-1
   for (int j = 0; j < k; j++) low = low && qubits[j] == j;
   out.k = k;
-  out.t7 = t7;
   out.mode = low ? kLowMode : (qubits[0] == 0 ? kPairMode : kColMode);
   out.renorm = (known_unitary || is_unitary(u, KA)) ? 1 : 0;
   const size_t img = k == 7   ? Tc7::IMG_BYTES
@@ -1748,8 +1260,7 @@ static void tc_prepare(const qcs_cuda_state *s, int k, const int *qubits_in, con
                               : TcShape<32>::IMG_BYTES;
   out.image_bytes = img + (size_t)KA * 8;
   out.image.assign(out.image_bytes, 0);
-  if (t7) make_image7_rows(u, out.image.data());
-  else if (k == 7) make_image7(u, out.image.data());
+  if (k == 7) make_image7(u, out.image.data());
   else if (k == 6) make_image<64>(u, out.image.data());
   else make_image<32>(u, out.image.data());
   float *rows = reinterpret_cast<float *>(out.image.data() + img);
@@ -1777,11 +1288,7 @@ static int tc_launch(qcs_cuda_state *s, const TcResident &b, const uint4 *img,
   const double *dsum = diffuse_in ? s->d_result + 4 : nullptr;
   ReduceSlot *sout = sum_out ? s->d_partials : nullptr;
   const TcGeom &g = b.g;
-  if (b.k == 7 && b.t7)
-    rc = b.mode == kLowMode    ? launch_tc7t<kLowMode>(s, g, img, b.renorm, dsum, sout)
-         : b.mode == kPairMode ? launch_tc7t<kPairMode>(s, g, img, b.renorm, dsum, sout)
-                               : launch_tc7t<kColMode>(s, g, img, b.renorm, dsum, sout);
-  else if (b.k == 7)
+  if (b.k == 7)
     rc = b.mode == kLowMode    ? launch_tc7<kLowMode>(s, g, img, b.renorm, dsum, sout)
          : b.mode == kPairMode ? launch_tc7<kPairMode>(s, g, img, b.renorm, dsum, sout)
                                : launch_tc7<kColMode>(s, g, img, b.renorm, dsum, sout);

@@ -88,46 +88,6 @@ __device__ __forceinline__ void umma_bf16(uint32_t d, uint64_t a, uint64_t b, ui
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
-// The same with A read from tensor memory (M rows = TMEM lanes, K packed two
-// bf16 per 32-bit column, the even element in the low half) and B from
-// shared memory.
-__device__ __forceinline__ void umma_bf16_ta(uint32_t d, uint32_t a_tmem, uint64_t b,
-                                             uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
-      "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-// 16 consecutive TMEM columns of this warp's 32 lanes from registers.
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t *r) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-      "%13,%14,%15,%16};" ::"r"(taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
-      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
-      "r"(r[15])
-      : "memory");
-}
-// Waits until this thread's tcgen05.st writes are done.
-__device__ __forceinline__ void tmem_wait_st() {
-  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-}
-// Named barrier `id` over `count` threads that also returns whether `pred`
-// holds in every one of them: a decision all of them take together.
-__device__ __forceinline__ bool bar_and(int id, int count, bool pred) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\tsetp.ne.b32 p, %1, 0;\n\t"
-      "bar.red.and.pred q, %2, %3, p;\n\tselp.b32 %0, 1, 0, q;\n}\n"
-      : "=r"(r)
-      : "r"((uint32_t)pred), "r"(id), "r"(count)
-      : "memory");
-  return r != 0;
-}
-__device__ __forceinline__ void bar_sync_n(int id, int count) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
 // Arrive on `bar` once every MMA issued so far by this thread has completed.
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile(
@@ -309,24 +269,6 @@ static void make_image7(const double *u, uint8_t *img) {
         op[2 * part + 1][off] = bf16_rn((float)(x - (double)bf16_to_float(h)));
       }
     }
-}
-
-// Block matrix u (128 x 128 complex, row-major) -> the four operands of the
-// k = 7 kernel that keeps the matrix in tensor memory: Re U hi, Re U lo,
-// Im U hi, Im U lo, each row-major (row = output, 128 bf16 inputs), so that
-// a thread owning row o loads 256 contiguous bytes per operand.
-static void make_image7_rows(const double *u, uint8_t *img) {
-  constexpr int KA = 128, U_BYTES = KA * KA * 2;
-  uint16_t *op[4];
-  for (int o = 0; o < 4; o++) op[o] = reinterpret_cast<uint16_t *>(img + o * U_BYTES);
-  for (int ao = 0; ao < KA; ao++)
-    for (int ai = 0; ai < KA; ai++)
-      for (int part = 0; part < 2; part++) {
-        const double x = u[2 * (ao * KA + ai) + part];
-        const uint16_t h = bf16_rn((float)x);
-        op[2 * part][ao * KA + ai] = h;
-        op[2 * part + 1][ao * KA + ai] = bf16_rn((float)(x - (double)bf16_to_float(h)));
-      }
 }
 
 }  // namespace qcs
