@@ -574,6 +574,17 @@ def run_sweeps(args, dist):
                 kk, q0 = int(name[8]), int(name.split("_at")[1])
                 ops[name] = ((lambda i, q=list(range(q0, q0 + kk)), u=us[kk]:
                               s.apply_block(q, u, capi.FUSE_TENSOR)), 2 * Ns)
+            # cphase_b<c>_<t>, phase_b<t>, cnot_b<c>_<t>: fixed bit placements
+            if name not in ops and name.startswith(("cphase_b", "phase_b", "cnot_b")):
+                bits = [int(b) for b in name.split("_b")[1].split("_")]
+                if name.startswith("cphase"):
+                    ops[name] = ((lambda i, c=bits[0], t=bits[1]:
+                                  s.apply_gate(W.CPHASE, t, c, 0.3)), Ns / 2)
+                elif name.startswith("cnot"):
+                    ops[name] = ((lambda i, c=bits[0], t=bits[1]:
+                                  s.apply_gate(W.CNOT, t, c)), Ns)
+                else:
+                    ops[name] = ((lambda i, t=bits[0]: s.apply_gate(W.P, t, -1, 0.3)), Ns)
             fn, nbytes = ops[name]
             for i in range(args.warmup):
                 fn(i)

@@ -16,6 +16,8 @@
 //
 // All kernels are grid-stride loops over 64-bit indices; each thread keeps
 // kUnroll independent pairs in flight to cover HBM latency.
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace qcs {
@@ -103,6 +105,34 @@ __global__ void __launch_bounds__(kSweepThreads)
   }
 }
 
+// complex64 with both bits above bit 0 (blo >= 1): the amplitudes 2x, 2x+1
+// of a 16-byte unit x share every bit but bit 0, so they are changed
+// together; unit p of the affected ones is x = p with zeros inserted at
+// blo-1 (and bhi-1), or'ed with setmask >> 1.  Four units in flight.
+__global__ void __launch_bounds__(kSweepThreads)
+    k_phase_mask_v2(float4 *v, i64 units, int blo, int bhi, i64 setmask, float2 phase) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p < units; p += kUnroll * nthr) {
+    float4 a[kUnroll];
+    i64 idx[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      i64 x = insert_zero(p + u * nthr, blo - 1);
+      if (bhi >= 0) x = insert_zero(x, bhi - 1);
+      idx[u] = x | (setmask >> 1);
+      if (p + u * nthr < units) a[u] = v[idx[u]];
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      if (p + u * nthr >= units) continue;
+      const float2 y0 = cmul(phase, make_float2(a[u].x, a[u].y));
+      const float2 y1 = cmul(phase, make_float2(a[u].z, a[u].w));
+      v[idx[u]] = make_float4(y0.x, y0.y, y1.x, y1.y);
+    }
+  }
+}
+
 // Unitary controlled-U, in place: pairs (lo, lo + 2^t) whose control bit is
 // set.  lo enumerates indices with bit c = 1 and bit t = 0.
 template <typename C>
@@ -131,6 +161,40 @@ __global__ void __launch_bounds__(kSweepThreads)
     C v0 = v[lo], v1 = v[lo + tb];
     v[lo] = cadd(cmul(m.g[0], v0), cmul(m.g[1], v1));
     v[lo + tb] = cadd(cmul(m.g[2], v0), cmul(m.g[3], v1));
+  }
+}
+
+// complex64 controlled-U with control and target above bit 0: pairs of
+// 16-byte units (lo, lo + 2^(t-1)), each unit two amplitudes that share the
+// control and target bits.  Same per-amplitude arithmetic as k_ctrl1q.
+__global__ void __launch_bounds__(kSweepThreads)
+    k_ctrl1q_v2(float4 *v, i64 npairs, int blo, int bhi, i64 cmask, int t, Mat2<float2> m) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  const i64 tb = 1LL << (t - 1);
+  i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p < npairs; p += kUnroll * nthr) {
+    float4 a[kUnroll], b[kUnroll];
+    i64 lo[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      lo[u] = insert_zero(insert_zero(p + u * nthr, blo - 1), bhi - 1) | (cmask >> 1);
+      if (p + u * nthr < npairs) {
+        a[u] = v[lo[u]];
+        b[u] = v[lo[u] + tb];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      if (p + u * nthr >= npairs) continue;
+      const float2 a0 = make_float2(a[u].x, a[u].y), a1 = make_float2(a[u].z, a[u].w);
+      const float2 b0 = make_float2(b[u].x, b[u].y), b1 = make_float2(b[u].z, b[u].w);
+      const float2 x0 = cadd(cmul(m.g[0], a0), cmul(m.g[1], b0));
+      const float2 x1 = cadd(cmul(m.g[0], a1), cmul(m.g[1], b1));
+      const float2 y0 = cadd(cmul(m.g[2], a0), cmul(m.g[3], b0));
+      const float2 y1 = cadd(cmul(m.g[2], a1), cmul(m.g[3], b1));
+      v[lo[u]] = make_float4(x0.x, x0.y, x1.x, x1.y);
+      v[lo[u] + tb] = make_float4(y0.x, y0.y, y1.x, y1.y);
+    }
   }
 }
 
@@ -194,8 +258,13 @@ static int apply_1q_t(qcs_cuda_state *s, const double m[8], int t) {
     if (is_one(m + 6)) return QCS_CUDA_OK;  // identity: 1*v + 0*v == v
     i64 cnt = s->size / 2;
     prof_begin(s);
-    k_phase_mask<C><<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads,
-                      0, s->stream>>>(v, cnt, t, -1, 1LL << t, g.g[3]);
+    if (std::is_same<C, float2>::value && t >= 1)
+      k_phase_mask_v2<<<grid_for(cnt / 2, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
+                        kSweepThreads, 0, s->stream>>>((float4 *)v, cnt / 2, t, -1, 1LL << t,
+                                                       make_float2((float)m[6], (float)m[7]));
+    else
+      k_phase_mask<C><<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
+                        kSweepThreads, 0, s->stream>>>(v, cnt, t, -1, 1LL << t, g.g[3]);
     return launched(s, KC_PHASE_MASK, Ns, "apply_1q (phase)");
   }
   if (diag) {
@@ -234,14 +303,25 @@ static int apply_ctrl_t(qcs_cuda_state *s, const double m[8], int c, int t) {
     if (is_one(m + 6)) return QCS_CUDA_OK;
     i64 cnt = s->size / 4;
     prof_begin(s);
-    k_phase_mask<C><<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads,
-                      0, s->stream>>>(v, cnt, blo, bhi, cmask | (1LL << t), g.g[3]);
+    if (std::is_same<C, float2>::value && blo >= 1)
+      k_phase_mask_v2<<<grid_for(cnt / 2, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
+                        kSweepThreads, 0, s->stream>>>((float4 *)v, cnt / 2, blo, bhi,
+                                                       cmask | (1LL << t),
+                                                       make_float2((float)m[6], (float)m[7]));
+    else
+      k_phase_mask<C><<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
+                        kSweepThreads, 0, s->stream>>>(v, cnt, blo, bhi, cmask | (1LL << t),
+                                                       g.g[3]);
     return launched(s, KC_PHASE_MASK, Ns / 2, "apply_controlled (phase)");
   }
   i64 np = s->size / 4;
   prof_begin(s);
-  k_ctrl1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads, 0,
-                s->stream>>>(v, np, blo, bhi, cmask, t, g);
+  if (std::is_same<C, float2>::value && blo >= 1)
+    k_ctrl1q_v2<<<grid_for(np / 2, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads,
+                  0, s->stream>>>((float4 *)v, np / 2, blo, bhi, cmask, t, to_mat2<float2>(m));
+  else
+    k_ctrl1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads, 0,
+                  s->stream>>>(v, np, blo, bhi, cmask, t, g);
   return launched(s, KC_CTRL1Q, Ns, "apply_controlled");
 }
 

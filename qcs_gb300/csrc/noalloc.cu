@@ -28,10 +28,11 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "sampler.cuh"
 
 namespace qcs {
 
-constexpr i64 kNoAllocTile = 4096;
+constexpr i64 kNoAllocTile = kSampleTile;
 constexpr i64 kNoAllocMaxTiles = 65536;
 
 static __device__ __align__(256) double g_noalloc_prefix[kNoAllocMaxTiles + 1];
@@ -58,122 +59,8 @@ static int noalloc_scratch(double **out) {
   return QCS_CUDA_OK;
 }
 
-template <typename C>
-__device__ __forceinline__ double na_prob(C x) {
-  return ((double)x.x * (double)x.x) + ((double)x.y * (double)x.y);
-}
-
-__device__ __forceinline__ double na_warp_sum(double x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  return x;
-}
-
-// A thread's share of a tile's probability mass, with the same arithmetic
-// as qcs_cuda_sample: FP64 for complex128; for complex64 an FP32 partial over
-// the thread's amplitudes, added in FP64.
-template <typename C>
-__device__ __forceinline__ double na_thread_mass(const C *v, i64 first, i64 tile) {
-  double a = 0.0;
-  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) a += na_prob(v[first + j]);
-  return a;
-}
-template <>
-__device__ __forceinline__ double na_thread_mass<float2>(const float2 *v, i64 first, i64 tile) {
-  float a = 0.f;
-  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) {
-    const float2 x = v[first + j];
-    a = fmaf(x.x, x.x, fmaf(x.y, x.y, a));
-  }
-  return (double)a;
-}
-
-// Probability mass of each tile into prefix[0..n_tiles).
-template <typename C>
-__global__ void __launch_bounds__(256)
-    k_na_tile_sums(const C *v, i64 tile, i64 n_tiles, double *prefix) {
-  __shared__ double part[8];
-  for (i64 t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-    double a = na_thread_mass<C>(v, t * tile, tile);
-    a = na_warp_sum(a);
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = a;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      double b = threadIdx.x < 8 ? part[threadIdx.x] : 0.0;
-      b = na_warp_sum(b);
-      if (threadIdx.x == 0) prefix[t] = b;
-    }
-    __syncthreads();
-  }
-}
-
-// In-place exclusive prefix of prefix[0..n), total into prefix[n].
-__global__ void __launch_bounds__(1024) k_na_prefix(double *x, i64 n) {
-  __shared__ double part[1024];
-  const i64 per = (n + blockDim.x - 1) / blockDim.x;
-  const i64 b = threadIdx.x * per;
-  const i64 e = b + per < n ? b + per : n;
-  double s = 0.0;
-  for (i64 i = b; i < e; i++) s += x[i];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double run = 0.0;
-    for (int k = 0; k < (int)blockDim.x; k++) {
-      double t = part[k];
-      part[k] = run;
-      run += t;
-    }
-    x[n] = run;
-  }
-  __syncthreads();
-  double run = part[threadIdx.x];
-  for (i64 i = b; i < e; i++) {
-    double t = x[i];
-    x[i] = run;
-    run += t;
-  }
-}
-
-// One warp per draw: binary search over the tile prefix, then an FP64 warp
-// scan of the chosen tile.  First index with r < running sum, or -1.
-template <typename C>
-__global__ void k_na_sample(const C *v, i64 tile, i64 n_tiles, const double *prefix,
-                            const double *draws, int shots, i64 *out) {
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int s = warp; s < shots; s += nwarps) {
-    const double r = draws[s];
-    i64 result = -1;
-    if (r < prefix[n_tiles]) {
-      i64 lo = 0, hi = n_tiles - 1;
-      while (lo < hi) {
-        i64 mid = (lo + hi) >> 1;
-        if (r < prefix[mid + 1]) hi = mid;
-        else lo = mid + 1;
-      }
-      double cum = prefix[lo];
-      i64 last_nonzero = lo * tile;
-      for (i64 base = lo * tile; base < (lo + 1) * tile && result < 0; base += 32) {
-        double p = lane < tile ? na_prob(v[base + lane]) : 0.0;
-        double incl = p;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          double y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        unsigned hit = __ballot_sync(0xffffffffu, lane < tile && r < cum + incl);
-        unsigned nz = __ballot_sync(0xffffffffu, lane < tile && p > 0.0);
-        if (hit) result = base + __ffs(hit) - 1;
-        else if (nz) last_nonzero = base + 31 - __clz(nz);
-        cum += __shfl_sync(0xffffffffu, incl, 31);
-      }
-      if (result < 0) result = last_nonzero;
-    }
-    if (lane == 0) out[s] = result;
-  }
-}
+// The kernels are those of qcs_cuda_sample (sampler.cuh): the same rule and
+// the same arithmetic, so both give the same indices for the same draws.
 
 // Forgets the current device's scratch address (after a failed launch).
 static void noalloc_forget() {
@@ -195,15 +82,15 @@ static int na_launch(const C *v, i64 count, const double *draws, int shots, i64 
                     "cudaDeviceGetAttribute(multiprocessor count)");
   if (rc) return rc;
   const int gt = (int)(n_tiles < (i64)sms * 8 ? n_tiles : (i64)sms * 8);
-  k_na_tile_sums<C><<<gt, 256, 0, st>>>(v, tile, n_tiles, prefix);
+  k_smp_tile_sums<C><<<gt, kSampleThreads, 0, st>>>(v, tile, n_tiles, prefix);
   rc = check_launch("sample_noalloc tile sums");
   if (rc) return rc;
-  k_na_prefix<<<1, 1024, 0, st>>>(prefix, n_tiles);
+  k_smp_prefix<<<1, 1024, 0, st>>>(prefix, n_tiles);
   rc = check_launch("sample_noalloc prefix");
   if (rc || shots == 0) return rc;
   int blocks = (int)(((i64)shots * 32 + 255) / 256);
   if (blocks > sms * 16) blocks = sms * 16;
-  k_na_sample<C><<<blocks, 256, 0, st>>>(v, tile, n_tiles, prefix, draws, shots, samples);
+  k_smp_sample<C><<<blocks, 256, 0, st>>>(v, tile, n_tiles, prefix, draws, shots, samples);
   return check_launch("sample_noalloc");
 }
 

@@ -12,6 +12,7 @@
 // grid is fixed per device, so every reduction is deterministic.  complex128
 // states use FP64 throughout.
 #include "common.cuh"
+#include "sampler.cuh"
 
 namespace qcs {
 
@@ -201,20 +202,59 @@ __global__ void __launch_bounds__(kSweepThreads)
 
 // Collapse after a measurement: amplitudes whose bit q differs from the
 // outcome become 0, the others are multiplied by `scale` when do_scale.
-template <typename C, typename R>
-__global__ void __launch_bounds__(kSweepThreads)
-    k_collapse(C *v, i64 size, int q, int outcome, R scale, int do_scale) {
+// complex64 in units of two amplitudes (one 16-byte access), four units in
+// flight per thread: for q >= 1 both amplitudes of a unit share bit q, so
+// the discarded half is written without being read, and the kept half is
+// read only when it is rescaled; for q = 0 each unit holds one of each.
+__global__ void __launch_bounds__(kReduceThreads)
+    k_collapse_c64(float4 *v, i64 units, int q, int outcome, float scale, int do_scale) {
   const i64 nthr = (i64)gridDim.x * blockDim.x;
-  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < size; i += nthr) {
-    if ((int)((i >> q) & 1) == outcome) {
-      if (do_scale) {
-        C x = v[i];
-        x.x *= scale;
-        x.y *= scale;
-        v[i] = x;
+  for (i64 u = (i64)blockIdx.x * blockDim.x + threadIdx.x; u < units; u += 4 * nthr) {
+    float4 x[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const i64 uu = u + k * nthr;
+      const bool keep = q == 0 || (int)(((2 * uu) >> q) & 1) == outcome;
+      if (uu < units && keep && (q == 0 || do_scale)) x[k] = v[uu];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const i64 uu = u + k * nthr;
+      if (uu >= units) continue;
+      if (q == 0) {
+        const float s = do_scale ? scale : 1.f;
+        v[uu] = outcome == 0 ? make_float4(x[k].x * s, x[k].y * s, 0.f, 0.f)
+                             : make_float4(0.f, 0.f, x[k].z * s, x[k].w * s);
+      } else if ((int)(((2 * uu) >> q) & 1) == outcome) {
+        if (do_scale)
+          v[uu] = make_float4(x[k].x * scale, x[k].y * scale, x[k].z * scale, x[k].w * scale);
+      } else {
+        v[uu] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
-    } else {
-      v[i] = make_c<C>(0.0, 0.0);
+    }
+  }
+}
+
+// complex128: one amplitude (16 bytes) per unit, four in flight per thread.
+__global__ void __launch_bounds__(kReduceThreads)
+    k_collapse_c128(double2 *v, i64 size, int q, int outcome, double scale, int do_scale) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < size; i += 4 * nthr) {
+    double2 x[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const i64 j = i + k * nthr;
+      if (j < size && do_scale && (int)((j >> q) & 1) == outcome) x[k] = v[j];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const i64 j = i + k * nthr;
+      if (j >= size) continue;
+      if ((int)((j >> q) & 1) == outcome) {
+        if (do_scale) v[j] = make_double2(x[k].x * scale, x[k].y * scale);
+      } else {
+        v[j] = make_double2(0.0, 0.0);
+      }
     }
   }
 }
@@ -280,6 +320,65 @@ __global__ void __launch_bounds__(kReduceThreads)
   }
 }
 
+// complex64: units of two amplitudes (one 16-byte load), four in flight per
+// thread; the same order (larger |a|^2, then smaller index) makes the result
+// independent of which thread saw which amplitude.
+__global__ void __launch_bounds__(kReduceThreads)
+    k_argmax_c64(const float4 *v, i64 units, ReduceSlot *out) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  float bv = -1.f;
+  i64 bi = 2 * units;
+  for (i64 u = (i64)blockIdx.x * blockDim.x + threadIdx.x; u < units; u += 4 * nthr) {
+    float4 x[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const i64 uu = u + k * nthr;
+      if (uu < units) x[k] = v[uu];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const i64 uu = u + k * nthr;
+      if (uu >= units) continue;
+      const float p0 = (x[k].x * x[k].x) + (x[k].y * x[k].y);
+      const float p1 = (x[k].z * x[k].z) + (x[k].w * x[k].w);
+      if (better(p0, 2 * uu, bv, bi)) {
+        bv = p0;
+        bi = 2 * uu;
+      }
+      if (better(p1, 2 * uu + 1, bv, bi)) {
+        bv = p1;
+        bi = 2 * uu + 1;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+    const i64 oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (better(ov, oi, bv, bi)) {
+      bv = ov;
+      bi = oi;
+    }
+  }
+  __shared__ float sv[kReduceThreads / 32];
+  __shared__ i64 si[kReduceThreads / 32];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sv[w] = bv;
+    si[w] = bi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); k++)
+      if (better(sv[k], si[k], bv, bi)) {
+        bv = sv[k];
+        bi = si[k];
+      }
+    out[blockIdx.x].a = (double)bv;
+    out[blockIdx.x].b = (double)bi;
+  }
+}
+
 __global__ void k_argmax_finalize(const ReduceSlot *p, int nblocks, double *result) {
   if (threadIdx.x != 0) return;
   double bv = -1.0, bi = 9.0e18;
@@ -292,120 +391,7 @@ __global__ void k_argmax_finalize(const ReduceSlot *p, int nblocks, double *resu
   result[1] = bi;
 }
 
-// ---- shot sampling -----------------------------------------------------------
-constexpr int kTile = 4096;
-
-template <typename C>
-__device__ __forceinline__ double prob64(C x) {
-  return ((double)x.x * (double)x.x) + ((double)x.y * (double)x.y);
-}
-
-// Per-tile probability mass.  complex128: FP64 throughout.  complex64: each
-// thread sums its amplitudes' |a|^2 in FP32 and adds that partial in FP64
-// (GB300's FP64 rate would otherwise bound this pass); a tile total off by
-// ~1e-7 of itself only moves that much mass onto the tile's last index in
-// k_sample's edge rule.
-template <typename C>
-__device__ __forceinline__ double thread_tile_mass(const C *v, i64 first, i64 tile) {
-  double a = 0.0;
-  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) a += prob64(v[first + j]);
-  return a;
-}
-template <>
-__device__ __forceinline__ double thread_tile_mass<float2>(const float2 *v, i64 first, i64 tile) {
-  float a = 0.f;
-  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) {
-    const float2 x = v[first + j];
-    a = fmaf(x.x, x.x, fmaf(x.y, x.y, a));
-  }
-  return (double)a;
-}
-
-template <typename C>
-__global__ void __launch_bounds__(kReduceThreads)
-    k_tile_sums(const C *v, i64 tile, i64 n_tiles, double *sums) {
-  for (i64 t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-    double a = thread_tile_mass<C>(v, t * tile, tile);
-    __shared__ ReduceSlot slot;
-    block_sum4(a, 0.0, 0.0, 0.0, &slot);
-    __syncthreads();
-    if (threadIdx.x == 0) sums[t] = slot.a;
-    __syncthreads();
-  }
-}
-
-// In-place exclusive prefix of n values (one block of 1024 threads, FP64,
-// fixed order); writes the total to x[n].
-__global__ void __launch_bounds__(1024) k_prefix(double *x, i64 n) {
-  __shared__ double part[1024];
-  const i64 per = (n + blockDim.x - 1) / blockDim.x;
-  const i64 b = threadIdx.x * per;
-  const i64 e = b + per < n ? b + per : n;
-  double s = 0.0;
-  for (i64 i = b; i < e; i++) s += x[i];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double run = 0.0;
-    for (int k = 0; k < (int)blockDim.x; k++) {
-      double t = part[k];
-      part[k] = run;
-      run += t;
-    }
-    x[n] = run;
-  }
-  __syncthreads();
-  double run = part[threadIdx.x];
-  for (i64 i = b; i < e; i++) {
-    double t = x[i];
-    x[i] = run;
-    run += t;
-  }
-}
-
-// One warp per draw r: find the tile whose inclusive prefix first exceeds r,
-// then scan it 32 amplitudes at a time with an FP64 warp prefix sum.  Result:
-// the first index with r < running sum (strict, as src/qcs.c:600), or -1.
-template <typename C>
-__global__ void k_sample(const C *v, i64 tile, i64 n_tiles, const double *prefix,
-                         const double *draws, int shots, i64 *out) {
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int s = warp; s < shots; s += nwarps) {
-    const double r = draws[s];
-    i64 result = -1;
-    if (r < prefix[n_tiles]) {
-      i64 lo = 0, hi = n_tiles - 1;  // smallest t with r < prefix[t+1]
-      while (lo < hi) {
-        i64 mid = (lo + hi) >> 1;
-        if (r < prefix[mid + 1]) hi = mid;
-        else lo = mid + 1;
-      }
-      double cum = prefix[lo];
-      i64 last_nonzero = lo * tile;
-      for (i64 base = lo * tile; base < (lo + 1) * tile && result < 0; base += 32) {
-        double p = 0.0;
-        if (lane < tile) p = prob64(v[base + lane]);
-        double incl = p;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          double y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        unsigned hit = __ballot_sync(0xffffffffu, lane < tile && r < cum + incl);
-        unsigned nz = __ballot_sync(0xffffffffu, lane < tile && p > 0.0);
-        if (hit) result = base + __ffs(hit) - 1;
-        else if (nz) last_nonzero = base + 31 - __clz(nz);
-        cum += __shfl_sync(0xffffffffu, incl, 31);
-      }
-      // r fell in this tile by its FP64 total but not by the element scan
-      // (rounding at the tile's upper edge): take its last non-empty index.
-      if (result < 0) result = last_nonzero;
-    }
-    if (lane == 0) out[s] = result;
-  }
-}
+// ---- shot sampling: sampler.cuh -------------------------------------------------
 
 // ---- host side -----------------------------------------------------------------
 
@@ -573,14 +559,13 @@ int qcs_cuda_measure(qcs_cuda_state *s, int qubit, double random_val, int *outco
   double kept = o ? r[1] : r[0];
   int do_scale = (kept > 1e-12 && kept != 1.0);
   double inv = do_scale ? 1.0 / sqrt(kept) : 1.0;
-  int g = grid_for(s->size, kSweepThreads, s->dev, 8);
   prof_begin(s);
   if (s->prec == QCS_CUDA_C128)
-    k_collapse<double2, double><<<g, kSweepThreads, 0, s->stream>>>((double2 *)s->vec, s->size,
-                                                                    qubit, o, inv, do_scale);
+    k_collapse_c128<<<s->dev.reduce_blocks, kReduceThreads, 0, s->stream>>>(
+        (double2 *)s->vec, s->size, qubit, o, inv, do_scale);
   else
-    k_collapse<float2, float><<<g, kSweepThreads, 0, s->stream>>>((float2 *)s->vec, s->size, qubit,
-                                                                  o, (float)inv, do_scale);
+    k_collapse_c64<<<s->dev.reduce_blocks, kReduceThreads, 0, s->stream>>>(
+        (float4 *)s->vec, s->size / 2, qubit, o, (float)inv, do_scale);
   invalidate_sum(s);
   rc = launched(s, KC_COLLAPSE, 1.5 * s->size * (s->prec == QCS_CUDA_C128 ? 16 : 8),
                 "measure collapse");
@@ -619,6 +604,9 @@ int qcs_cuda_argmax(qcs_cuda_state *s, long long *index, double *prob) {
   if (s->prec == QCS_CUDA_C128)
     k_argmax<double2, double><<<d.reduce_blocks, kReduceThreads, 0, s->stream>>>(
         (const double2 *)s->vec, s->size, s->d_partials);
+  else if (s->size >= 2)
+    k_argmax_c64<<<d.reduce_blocks, kReduceThreads, 0, s->stream>>>(
+        (const float4 *)s->vec, s->size / 2, s->d_partials);
   else
     k_argmax<float2, float><<<d.reduce_blocks, kReduceThreads, 0, s->stream>>>(
         (const float2 *)s->vec, s->size, s->d_partials);
@@ -650,15 +638,15 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
   const double sb = s->prec == QCS_CUDA_C128 ? 16 : 8;
   prof_begin(s);
   if (s->prec == QCS_CUDA_C128)
-    k_tile_sums<double2><<<gt, kReduceThreads, 0, s->stream>>>((const double2 *)s->vec, tile,
-                                                              s->n_tiles, s->d_tile_prefix);
+    k_smp_tile_sums<double2><<<gt, kSampleThreads, 0, s->stream>>>(
+        (const double2 *)s->vec, tile, s->n_tiles, s->d_tile_prefix);
   else
-    k_tile_sums<float2><<<gt, kReduceThreads, 0, s->stream>>>((const float2 *)s->vec, tile,
-                                                             s->n_tiles, s->d_tile_prefix);
+    k_smp_tile_sums<float2><<<gt, kSampleThreads, 0, s->stream>>>(
+        (const float2 *)s->vec, tile, s->n_tiles, s->d_tile_prefix);
   rc = launched(s, KC_SAMPLE, s->size * sb, "sample tile sums");
   if (rc) return rc;
   prof_begin(s);
-  k_prefix<<<1, 1024, 0, s->stream>>>(s->d_tile_prefix, s->n_tiles);
+  k_smp_prefix<<<1, 1024, 0, s->stream>>>(s->d_tile_prefix, s->n_tiles);
   rc = launched(s, KC_SAMPLE, 16.0 * s->n_tiles, "sample prefix");
   if (rc) return rc;
   memcpy(s->h_draws, random_vals, (size_t)shots * sizeof(double));
@@ -669,13 +657,13 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
   if (blocks > d.num_sms * 16) blocks = d.num_sms * 16;
   prof_begin(s);
   if (s->prec == QCS_CUDA_C128)
-    k_sample<double2><<<blocks, threads, 0, s->stream>>>((const double2 *)s->vec, tile, s->n_tiles,
-                                                        s->d_tile_prefix, s->d_draws, shots,
-                                                        s->d_samples);
+    k_smp_sample<double2><<<blocks, threads, 0, s->stream>>>(
+        (const double2 *)s->vec, tile, s->n_tiles, s->d_tile_prefix, s->d_draws, shots,
+        s->d_samples);
   else
-    k_sample<float2><<<blocks, threads, 0, s->stream>>>((const float2 *)s->vec, tile, s->n_tiles,
-                                                       s->d_tile_prefix, s->d_draws, shots,
-                                                       s->d_samples);
+    k_smp_sample<float2><<<blocks, threads, 0, s->stream>>>(
+        (const float2 *)s->vec, tile, s->n_tiles, s->d_tile_prefix, s->d_draws, shots,
+        s->d_samples);
   rc = launched(s, KC_SAMPLE, (double)shots * tile * sb, "sample");
   if (!rc) rc = copy_d2h(s, s->h_samples, s->d_samples, (size_t)shots * sizeof(i64),
                          "sample readback");

@@ -1,0 +1,189 @@
+// sampler.cuh -- the kernels of shot sampling (qc_run_shots, src/qcs.c:575-607):
+// per-tile probability masses, their exclusive prefix, and one warp per draw.
+// Shared by qcs_cuda_sample (per-state scratch) and qcs_cuda_sample_noalloc
+// (a fixed library array), so that both give the same indices for the same
+// draws.  The kernels have internal linkage: each translation unit that
+// includes this header has its own copy.
+#pragma once
+
+#include "common.cuh"
+
+namespace qcs {
+namespace {
+
+constexpr i64 kSampleTile = 4096;    // amplitudes per tile of the prefix
+constexpr int kSampleThreads = 256;  // threads of the tile-sum blocks
+
+__device__ __forceinline__ double smp_warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+template <typename C>
+__device__ __forceinline__ double smp_prob(C x) {
+  return ((double)x.x * (double)x.x) + ((double)x.y * (double)x.y);
+}
+
+// A thread's share of a full tile's probability mass: complex64 as 8 float4
+// loads issued together (units t, t + 256, ... of the tile's 2048 pairs of
+// amplitudes), |a|^2 summed in FP32 in that order and returned in FP64;
+// complex128 as 16 double2 loads, FP64 throughout.
+template <typename C>
+__device__ __forceinline__ double smp_full_tile_mass(const C *v, i64 first);
+template <>
+__device__ __forceinline__ double smp_full_tile_mass<float2>(const float2 *v, i64 first) {
+  constexpr int U = (int)(kSampleTile / 2 / kSampleThreads);  // 8
+  const float4 *p = reinterpret_cast<const float4 *>(v + first) + threadIdx.x;
+  float4 x[U];
+#pragma unroll
+  for (int k = 0; k < U; k++) x[k] = p[k * kSampleThreads];
+  float a = 0.f;
+#pragma unroll
+  for (int k = 0; k < U; k++) {
+    a = fmaf(x[k].x, x[k].x, fmaf(x[k].y, x[k].y, a));
+    a = fmaf(x[k].z, x[k].z, fmaf(x[k].w, x[k].w, a));
+  }
+  return (double)a;
+}
+template <>
+__device__ __forceinline__ double smp_full_tile_mass<double2>(const double2 *v, i64 first) {
+  constexpr int U = (int)(kSampleTile / kSampleThreads);  // 16
+  const double2 *p = v + first + threadIdx.x;
+  double2 x[U];
+#pragma unroll
+  for (int k = 0; k < U; k++) x[k] = p[k * kSampleThreads];
+  double a = 0.0;
+#pragma unroll
+  for (int k = 0; k < U; k++) a += smp_prob(x[k]);
+  return a;
+}
+
+// The same for a state smaller than one full tile (its single tile).
+template <typename C>
+__device__ __forceinline__ double smp_small_tile_mass(const C *v, i64 tile) {
+  double a = 0.0;
+  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) a += smp_prob(v[j]);
+  return a;
+}
+template <>
+__device__ __forceinline__ double smp_small_tile_mass<float2>(const float2 *v, i64 tile) {
+  float a = 0.f;
+  for (i64 j = threadIdx.x; j < tile; j += blockDim.x) {
+    const float2 x = v[j];
+    a = fmaf(x.x, x.x, fmaf(x.y, x.y, a));
+  }
+  return (double)a;
+}
+
+// Probability mass of each tile into sums[0 .. n_tiles): one block per tile
+// at a time, FP64 across the block's threads in a fixed order.
+template <typename C>
+__global__ void __launch_bounds__(kSampleThreads)
+    k_smp_tile_sums(const C *v, i64 tile, i64 n_tiles, double *sums) {
+  __shared__ double part[kSampleThreads / 32];
+  for (i64 t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    double a = tile == kSampleTile ? smp_full_tile_mass<C>(v, t * kSampleTile)
+                                   : smp_small_tile_mass<C>(v, tile);
+    a = smp_warp_sum(a);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double b = threadIdx.x < kSampleThreads / 32 ? part[threadIdx.x] : 0.0;
+      b = smp_warp_sum(b);
+      if (threadIdx.x == 0) sums[t] = b;
+    }
+    __syncthreads();
+  }
+}
+
+// In-place exclusive prefix of x[0 .. n) (one block of 1024 threads, FP64,
+// fixed order: each thread a contiguous segment, then the segment totals);
+// the total goes to x[n].
+__global__ void __launch_bounds__(1024) k_smp_prefix(double *x, i64 n) {
+  __shared__ double seg[1024];
+  const i64 per = (n + blockDim.x - 1) / blockDim.x;
+  const i64 b = threadIdx.x * per;
+  const i64 e = b + per < n ? b + per : n;
+  double s = 0.0;
+#pragma unroll 8
+  for (i64 i = b; i < e; i++) s += x[i];
+  seg[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double run = 0.0;
+    for (int k = 0; k < (int)blockDim.x; k++) {
+      const double t = seg[k];
+      seg[k] = run;
+      run += t;
+    }
+    x[n] = run;
+  }
+  __syncthreads();
+  double run = seg[threadIdx.x];
+  for (i64 i = b; i < e; i++) {
+    const double t = x[i];
+    x[i] = run;
+    run += t;
+  }
+}
+
+// One warp per draw r: the tile whose inclusive prefix first exceeds r (a
+// binary search), then an FP64 scan of that tile 32 amplitudes at a time
+// (four groups' loads in flight together).  Result: the first index with
+// r < running sum (strict, as src/qcs.c:600), or -1 when r is not below the
+// total.  When r falls in a tile by its total but not by the element scan
+// (rounding at the tile's upper edge), the tile's last nonzero index.
+template <typename C>
+__global__ void k_smp_sample(const C *v, i64 tile, i64 n_tiles, const double *prefix,
+                             const double *draws, int shots, i64 *out) {
+  constexpr int G = 4;  // 32-amplitude groups loaded together
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = warp; s < shots; s += nwarps) {
+    const double r = draws[s];
+    i64 result = -1;
+    if (r < prefix[n_tiles]) {
+      i64 lo = 0, hi = n_tiles - 1;  // smallest t with r < prefix[t + 1]
+      while (lo < hi) {
+        const i64 mid = (lo + hi) >> 1;
+        if (r < prefix[mid + 1]) hi = mid;
+        else lo = mid + 1;
+      }
+      double cum = prefix[lo];
+      i64 last_nonzero = lo * tile;
+      const i64 end = (lo + 1) * tile;
+      for (i64 base = lo * tile; base < end && result < 0; base += 32 * G) {
+        double p[G];
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+          const i64 i = base + 32 * k + lane;
+          p[k] = i < end ? smp_prob(v[i]) : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+          const i64 gb = base + 32 * k;
+          if (result >= 0 || gb >= end) break;  // warp-uniform
+          double incl = p[k];
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const bool valid = gb + lane < end;
+          const unsigned hit = __ballot_sync(0xffffffffu, valid && r < cum + incl);
+          const unsigned nz = __ballot_sync(0xffffffffu, valid && p[k] > 0.0);
+          if (hit) result = gb + __ffs(hit) - 1;
+          else if (nz) last_nonzero = gb + 31 - __clz(nz);
+          cum += __shfl_sync(0xffffffffu, incl, 31);
+        }
+      }
+      if (result < 0) result = last_nonzero;
+    }
+    if (lane == 0) out[s] = result;
+  }
+}
+
+}  // namespace
+}  // namespace qcs
