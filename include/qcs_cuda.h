@@ -114,6 +114,15 @@ int qcs_cuda_device_count(int *count);
  * allocations (what == 1) or kernel launches (what == 2) report failure
  * without touching the GPU.  what == 0 clears it. */
 int qcs_cuda_debug_inject(int what, int count);
+/* Clock-cycle limit of the bounded device-side waits in kernels launched
+ * from now on (the tensor-core pipelines' handoffs and the batched kernel's
+ * CTA-group counters): cycles > 0 sets it, cycles == 0 restores the default
+ * (about 2 s).  For tests of the timeout path: a wait that runs out raises
+ * the device error flag, its CTA leaves its loops and releases what it
+ * holds, and the next qcs_cuda_synchronize (or batch run) returns
+ * QCS_CUDA_ETIMEOUT.  No counterpart in the reference (it has no device
+ * code). */
+int qcs_cuda_debug_set_wait_cycles(long long cycles);
 
 /* ---- state lifecycle ---------------------------------------------------
  * Replaces q_state_init / q_state_free (src/q_state.c:32-115) and the

@@ -73,6 +73,7 @@ def _declare(L):
         "qcs_cuda_last_error": (C.c_char_p, []),
         "qcs_cuda_device_count": (i, [ip]),
         "qcs_cuda_debug_inject": (i, [i, i]),
+        "qcs_cuda_debug_set_wait_cycles": (i, [ll]),
         "qcs_cuda_state_create": (i, [i, i, i, vpp]),
         "qcs_cuda_state_destroy": (i, [vp]),
         "qcs_cuda_state_info": (i, [vp, ip, ip, ip]),

@@ -52,7 +52,6 @@ struct BInst {
 };
 
 // Bounded spin of one thread on a counter another CTA raises: ~2 s.
-constexpr long long kBatchWaitCycles = 4000000000LL;
 
 struct BStage {
   int group0;
@@ -130,6 +129,7 @@ struct qcs_cuda_batch {
   qcs::i64 *h_samples;  // pinned
   float2 *d_slots;      // one global slot per CTA for instances above tile_q
   int *d_err;
+  long long wait_captured;  // wait limit the captured graph's kernel carries
   size_t slot_amps;
   int grid;
   size_t cap_gates, cap_stages;
@@ -325,12 +325,13 @@ __device__ void smem_prefix(double *x, int m) {
   __syncthreads();
 }
 
-// Thread 0 waits until *cnt >= target (bounded); false on timeout or abort.
-__device__ bool wait_count(const int *cnt, int target, int *err, int where) {
+// Thread 0 waits until *cnt >= target, at most `limit` clock cycles; false
+// on timeout or abort.
+__device__ bool wait_count(const int *cnt, int target, int *err, int where, long long limit) {
   const long long t0 = clock64();
   while (*(volatile const int *)cnt < target) {
     if (*(volatile const int *)err) return false;
-    if (clock64() - t0 > kBatchWaitCycles) {
+    if (clock64() - t0 > limit) {
       atomicCAS(err, 0, where);
       return false;
     }
@@ -350,7 +351,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
     k_batch(const BInst *insts, const BStage *stages, const BGroup *groups, const BGate *gates,
             const int2 *items, int n_items, int shots, u64 seed, int tile_q, float2 *slots,
             i64 slot_amps, int *queue, int *stage_done, int *lead, int *err, double *z_out,
-            i64 *samples_out) {
+            i64 *samples_out, long long wait) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *S = reinterpret_cast<float2 *>(smem_raw);               // 2^tile_q amplitudes
   double *prefix = reinterpret_cast<double *>(S + (1 << tile_q));  // up to 1025 tile masses
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
         if (member == 0) {
           atomicExch(&lead[inst], blockIdx.x + 1);
         } else {
-          s_ok = wait_count(&lead[inst], 1, err, 1) ? 1 : 0;
+          s_ok = wait_count(&lead[inst], 1, err, 1, wait) ? 1 : 0;
         }
       }
       __syncthreads();
@@ -475,7 +476,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
           if (threadIdx.x == 0) {
             __threadfence();
             atomicAdd(&stage_done[inst], 1);
-            s_ok = wait_count(&stage_done[inst], G * (si + 1), err, 2) ? 1 : 0;
+            s_ok = wait_count(&stage_done[inst], G * (si + 1), err, 2, wait) ? 1 : 0;
           }
           __syncthreads();
           if (!s_ok) return;
@@ -797,7 +798,7 @@ static int batch_enqueue(qcs_cuda_batch *b) {
   k_batch<T><<<b->grid, T, smem, b->stream>>>(                                                    \
       b->d_insts, b->d_stages, b->d_groups, b->d_gates, b->d_items, (int)b->items.size(),           \
       b->shots, b->seed, tq, b->d_slots, (i64)b->slot_amps, b->d_queue, b->d_stage_done, b->d_lead, \
-      b->d_err, b->d_z, b->d_samples)
+      b->d_err, b->d_z, b->d_samples, b->wait_captured)
   switch (b->tune.threads) {
     case 256: QCS_LAUNCH_BATCH(256); break;
     case 512: QCS_LAUNCH_BATCH(512); break;
@@ -812,6 +813,7 @@ static int batch_enqueue(qcs_cuda_batch *b) {
 }
 
 static int batch_capture(qcs_cuda_batch *b) {
+  b->wait_captured = wait_cycles();  // the graph's kernel node keeps this limit
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
@@ -975,7 +977,9 @@ int qcs_cuda_batch_set_angles(qcs_cuda_batch *b, const double *angles) {
 int qcs_cuda_batch_run(qcs_cuda_batch *b, double *expect_z0, long long *samples, double *ms) {
   if (!b) return set_error(QCS_CUDA_EINVAL, "null batch");
   float t = 0.f;
-  int rc = batch_launch_checked(b, &t);
+  int rc = QCS_CUDA_OK;
+  if (b->wait_captured != wait_cycles()) rc = batch_capture(b);  // the wait limit changed
+  if (!rc) rc = batch_launch_checked(b, &t);
   if (rc) return rc;
   b->last_ms = t;
   if (ms) *ms = t;

@@ -210,7 +210,8 @@ __device__ __forceinline__ TileWalk tile_walk(const TcGeom &g) {
 template <int KA, int MODE, bool FUSED>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_block_tc(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
-               const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err) {
+               const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err,
+               long long wait) {
   using S = TcShape<KA>;
   extern __shared__ uint8_t smem_dyn[];
   const uint32_t raw = smem_u32(smem_dyn);
@@ -374,7 +375,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (p < g.nruns && it + g.pf_ahead < w.count)  // nruns <= 128 < 256 producers
         prefetch_l2(v + tile_base(w.at(it + g.pf_ahead), g) + g.run_off[p],
                     (uint32_t)g.run_bytes);
-      if (it >= 2 && !wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1)) break;
+      // every lane of a warp takes the same decision (the low-mode norm
+      // exchange below is a full-warp shuffle)
+      if (it >= 2 &&
+          !__all_sync(0xffffffffu, wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err,
+                                            1, wait)))
+        break;
       uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
       uint8_t *alo = ahi + S::A_BYTES;
       float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
@@ -427,8 +433,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const TileWalk w = tile_walk(g);
       for (int it = 0; it < w.count; ++it) {
         const int stage = it & 1;
-        if (!wait_bar(bar(stage), (it >> 1) & 1, abort_flag, err, 2)) break;
-        if (it >= 2 && !wait_bar(bar(4 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 3)) break;
+        if (!wait_bar(bar(stage), (it >> 1) & 1, abort_flag, err, 2, wait)) break;
+        if (it >= 2 && !wait_bar(bar(4 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 3, wait))
+          break;
         tc_fence_after();
         const uint32_t d = tmem + (uint32_t)(stage * S::N);
         const uint32_t a_hi = a0 + (uint32_t)(2 * stage * S::A_BYTES);
@@ -491,10 +498,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int it = 0; it < w.count; ++it) {
       const i64 tile = w.at(it);
       const int stage = it & 1;
-      if (!wait_bar(bar(2 + stage), (it >> 1) & 1, abort_flag, err, 5)) break;
+      bool ok = wait_bar(bar(2 + stage), (it >> 1) & 1, abort_flag, err, 5, wait);
       // this tile's column norms; slot it % 4 cannot be refilled before this
       // epilogue arrives on acc_empty, so its phase is unambiguous
-      if (!wait_bar(bar(7 + it % kSqSlots), (it / kSqSlots) & 1, abort_flag, err, 6)) break;
+      ok = ok && wait_bar(bar(7 + it % kSqSlots), (it / kSqSlots) & 1, abort_flag, err, 6, wait);
+      if (!__all_sync(0xffffffffu, ok)) break;  // the warp's TMEM loads are .sync.aligned
       tc_fence_after();
       const uint32_t tb = tmem + lane_addr + (uint32_t)(stage * S::N);
       float scale = 1.f;
@@ -618,7 +626,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 template <int MODE, bool FUSED>
 __global__ void __launch_bounds__(Tc7::THREADS, 1)
     k_block_tc7(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
-                const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err) {
+                const double *diffuse_sum, double inv_n, ReduceSlot *sum_out, int *err,
+                long long wait) {
   using S = Tc7;
   extern __shared__ uint8_t smem_dyn[];
   const uint32_t raw = smem_u32(smem_dyn);
@@ -809,7 +818,8 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
         prefetch_l2(v + tile_base(w.at(it + g.pf_ahead), g) + g.run_off[p],
                     (uint32_t)g.run_bytes);
       // stage b is free once the MMAs of chunk q - 2 are done
-      if (q >= 2 && !wait_bar(bar(2 + b), (uint32_t)(((q - 2) >> 1) & 1), abort_flag, err, 1))
+      if (q >= 2 && !__all_sync(0xffffffffu, wait_bar(bar(2 + b), (uint32_t)(((q - 2) >> 1) & 1),
+                                                       abort_flag, err, 1, wait)))
         return false;
       if (c == 0) {
         part = 0.f;
@@ -843,13 +853,13 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
       for (i64 it = 0; ok && it < w.count; ++it) {
         const int acc_st = (int)(it & 1);
         if (it >= 2 &&
-            !wait_bar(bar(6 + acc_st), (uint32_t)(((it - 2) >> 1) & 1), abort_flag, err, 3))
+            !wait_bar(bar(6 + acc_st), (uint32_t)(((it - 2) >> 1) & 1), abort_flag, err, 3, wait))
           break;
         const uint32_t dr = tmem + (uint32_t)(acc_st * 2 * S::N), di = dr + (uint32_t)S::N;
         for (int c = 0; c < S::CHUNKS; c++) {
           const i64 q = it * S::CHUNKS + c;
           const int b = (int)(q & 1);
-          if (!wait_bar(bar(b), (uint32_t)((q >> 1) & 1), abort_flag, err, 2)) {
+          if (!wait_bar(bar(b), (uint32_t)((q >> 1) & 1), abort_flag, err, 2, wait)) {
             ok = false;
             break;
           }
@@ -905,10 +915,10 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
     for (i64 it = 0; it < w.count; ++it) {
       const i64 tile = w.at(it);
       const int acc_st = (int)(it & 1);
-      if (!wait_bar(bar(4 + acc_st), (uint32_t)((it >> 1) & 1), abort_flag, err, 5)) break;
-      if (!wait_bar(bar(9 + (int)(it % kSqSlots)), (uint32_t)((it / kSqSlots) & 1), abort_flag,
-                    err, 6))
-        break;
+      bool ok = wait_bar(bar(4 + acc_st), (uint32_t)((it >> 1) & 1), abort_flag, err, 5, wait);
+      ok = ok && wait_bar(bar(9 + (int)(it % kSqSlots)), (uint32_t)((it / kSqSlots) & 1),
+                          abort_flag, err, 6, wait);
+      if (!__all_sync(0xffffffffu, ok)) break;  // the warp's TMEM loads are .sync.aligned
       tc_fence_after();
       const uint32_t tr = tmem + lane_addr + (uint32_t)(acc_st * 2 * S::N);
       const uint32_t ti = tr + (uint32_t)S::N;
@@ -1073,10 +1083,11 @@ static int launch_tc(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int r
   prof_begin(s);
   if (diffuse_sum || sum_out)
     k_block_tc<KA, MODE, true><<<grid, kTcThreads, S::SMEM, s->stream>>>(
-        (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err);
+        (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err,
+        wait_cycles());
   else
     k_block_tc<KA, MODE, false><<<grid, kTcThreads, S::SMEM, s->stream>>>(
-        (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err);
+        (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err, wait_cycles());
   return launched(s, KC_BLOCK_TC, 2.0 * s->size * 8.0, "apply_block (tcgen05)");
 }
 
@@ -1099,10 +1110,11 @@ static int launch_tc7(qcs_cuda_state *s, const TcGeom &g, const uint4 *img, int 
   prof_begin(s);
   if (diffuse_sum || sum_out)
     k_block_tc7<MODE, true><<<grid, Tc7::THREADS, Tc7::SMEM, s->stream>>>(
-        (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err);
+        (float2 *)s->vec, g, img, renorm, diffuse_sum, ldexp(1.0, -s->n), sum_out, s->d_err,
+        wait_cycles());
   else
     k_block_tc7<MODE, false><<<grid, Tc7::THREADS, Tc7::SMEM, s->stream>>>(
-        (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err);
+        (float2 *)s->vec, g, img, renorm, nullptr, 0.0, nullptr, s->d_err, wait_cycles());
   return launched(s, KC_BLOCK_TC7, 2.0 * s->size * 8.0, "apply_block (tcgen05, k = 7)");
 }
 

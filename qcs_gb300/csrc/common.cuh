@@ -128,6 +128,11 @@ int launched(qcs_cuda_state *s, int cls, double bytes, const char *what);
 // allocation / launch must report failure.
 bool inject_alloc_failure();
 bool inject_launch_failure();
+// Clock-cycle limit of the bounded device-side waits (pipeline handoffs,
+// CTA-group counters) of kernels launched from now on: kDefaultWaitCycles
+// (~2 s) unless qcs_cuda_debug_set_wait_cycles set another.
+constexpr long long kDefaultWaitCycles = 4000000000LL;
+long long wait_cycles();
 int device_info(int device, DeviceInfo *out);
 
 // ---- complex helpers --------------------------------------------------------

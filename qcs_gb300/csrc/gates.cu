@@ -133,6 +133,32 @@ __global__ void __launch_bounds__(kSweepThreads)
   }
 }
 
+// complex64 with the lower bit at bit 0 (blo == 0): the odd amplitude of
+// every 16-byte unit whose bit bhi - 1 is set (bhi < 0: of every unit) gets
+// the phase.  Whole units are moved, so a warp's accesses fill the 32-byte
+// sectors the touched amplitudes lie in.
+__global__ void __launch_bounds__(kSweepThreads)
+    k_phase_mask_odd(float4 *v, i64 units, int bhi, float2 phase) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  const i64 set = bhi >= 1 ? 1LL << (bhi - 1) : 0;
+  i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p < units; p += kUnroll * nthr) {
+    float4 a[kUnroll];
+    i64 idx[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      idx[u] = bhi >= 1 ? (insert_zero(p + u * nthr, bhi - 1) | set) : p + u * nthr;
+      if (p + u * nthr < units) a[u] = v[idx[u]];
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      if (p + u * nthr >= units) continue;
+      const float2 y = cmul(phase, make_float2(a[u].z, a[u].w));
+      v[idx[u]] = make_float4(a[u].x, a[u].y, y.x, y.y);
+    }
+  }
+}
+
 // Unitary controlled-U, in place: pairs (lo, lo + 2^t) whose control bit is
 // set.  lo enumerates indices with bit c = 1 and bit t = 0.
 template <typename C>
@@ -262,6 +288,10 @@ static int apply_1q_t(qcs_cuda_state *s, const double m[8], int t) {
       k_phase_mask_v2<<<grid_for(cnt / 2, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
                         kSweepThreads, 0, s->stream>>>((float4 *)v, cnt / 2, t, -1, 1LL << t,
                                                        make_float2((float)m[6], (float)m[7]));
+    else if (std::is_same<C, float2>::value)  // t == 0
+      k_phase_mask_odd<<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
+                         kSweepThreads, 0, s->stream>>>((float4 *)v, cnt, -1,
+                                                        make_float2((float)m[6], (float)m[7]));
     else
       k_phase_mask<C><<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
                         kSweepThreads, 0, s->stream>>>(v, cnt, t, -1, 1LL << t, g.g[3]);
@@ -308,6 +338,10 @@ static int apply_ctrl_t(qcs_cuda_state *s, const double m[8], int c, int t) {
                         kSweepThreads, 0, s->stream>>>((float4 *)v, cnt / 2, blo, bhi,
                                                        cmask | (1LL << t),
                                                        make_float2((float)m[6], (float)m[7]));
+    else if (std::is_same<C, float2>::value)  // blo == 0: units with bit bhi set
+      k_phase_mask_odd<<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
+                         kSweepThreads, 0, s->stream>>>((float4 *)v, cnt, bhi,
+                                                        make_float2((float)m[6], (float)m[7]));
     else
       k_phase_mask<C><<<grid_for(cnt, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
                         kSweepThreads, 0, s->stream>>>(v, cnt, blo, bhi, cmask | (1LL << t),

@@ -105,9 +105,16 @@ __global__ void __launch_bounds__(1024) k_smp_prefix(double *x, i64 n) {
   const i64 per = (n + blockDim.x - 1) / blockDim.x;
   const i64 b = threadIdx.x * per;
   const i64 e = b + per < n ? b + per : n;
+  constexpr int B = 8;  // loads in flight per thread
   double s = 0.0;
-#pragma unroll 8
-  for (i64 i = b; i < e; i++) s += x[i];
+  for (i64 i0 = b; i0 < e; i0 += B) {
+    double t[B];
+#pragma unroll
+    for (int k = 0; k < B; k++) t[k] = i0 + k < e ? x[i0 + k] : 0.0;
+#pragma unroll
+    for (int k = 0; k < B; k++)
+      if (i0 + k < e) s += t[k];
+  }
   seg[threadIdx.x] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -121,10 +128,16 @@ __global__ void __launch_bounds__(1024) k_smp_prefix(double *x, i64 n) {
   }
   __syncthreads();
   double run = seg[threadIdx.x];
-  for (i64 i = b; i < e; i++) {
-    const double t = x[i];
-    x[i] = run;
-    run += t;
+  for (i64 i0 = b; i0 < e; i0 += B) {
+    double t[B];
+#pragma unroll
+    for (int k = 0; k < B; k++) t[k] = i0 + k < e ? x[i0 + k] : 0.0;
+#pragma unroll
+    for (int k = 0; k < B; k++)
+      if (i0 + k < e) {
+        x[i0 + k] = run;
+        run += t[k];
+      }
   }
 }
 

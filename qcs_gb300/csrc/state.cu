@@ -20,6 +20,7 @@ namespace qcs {
 static thread_local char g_last_error[512] = "";
 static std::atomic<int> g_inject_alloc{0};
 static std::atomic<int> g_inject_launch{0};
+static std::atomic<long long> g_wait_cycles{0};  // 0: kDefaultWaitCycles
 
 int set_error(int status, const char *fmt, ...) {
   va_list ap;
@@ -43,6 +44,11 @@ int check_launch(const char *what) {
     return set_error(QCS_CUDA_ELAUNCH, "%s: injected launch failure", what);
   }
   return check_cuda(cudaGetLastError(), what);
+}
+
+long long wait_cycles() {
+  const long long w = g_wait_cycles.load();
+  return w > 0 ? w : kDefaultWaitCycles;
 }
 
 static bool take_one(std::atomic<int> &c) {
@@ -279,6 +285,12 @@ int qcs_cuda_device_count(int *count) {
     c = 0;
   }
   *count = c;
+  return QCS_CUDA_OK;
+}
+
+int qcs_cuda_debug_set_wait_cycles(long long cycles) {
+  if (cycles < 0) return set_error(QCS_CUDA_EINVAL, "negative wait limit");
+  g_wait_cycles = cycles;
   return QCS_CUDA_OK;
 }
 

@@ -13,7 +13,9 @@
 namespace qcs {
 
 constexpr int kTcM = 128;                       // state columns per tile = UMMA M = TMEM lanes
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+// The final drain of a kernel's MMAs always waits this long (its MMAs
+// complete in microseconds); the pipeline waits take the launch's limit.
+constexpr long long kWaitCycles = kDefaultWaitCycles;  // ~2 s at 2 GHz
 
 // Byte offset of bf16 element (r, k) in a K-major operand of R rows laid out
 // in 128-byte swizzle atoms (8 rows x 64 elements, 16-byte chunks permuted by
@@ -196,14 +198,16 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
          ((uint32_t)(M >> 4) << 24);
 }
 
-// Bounded mbarrier wait.  Returns false when the CTA is aborting.
+// Bounded mbarrier wait: at most `limit` clock cycles (the launch's wait
+// limit, kWaitCycles unless a debug override shortened it).  Returns false
+// when the CTA is aborting.
 static __device__ __noinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int *abort_flag,
-                                      int *err, int where) {
+                                      int *err, int where, long long limit) {
   long long t0 = clock64();
   for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
-    if (clock64() - t0 > kWaitCycles) {
+    if (clock64() - t0 > limit) {
       *abort_flag = 1;
       atomicExch(err, where);
       return false;

@@ -56,6 +56,13 @@ def test_debug_inject_arguments():
     assert L.qcs_cuda_debug_inject(0, 0) == capi.OK
 
 
+def test_debug_wait_limit_arguments():
+    L = capi.lib()
+    assert L.qcs_cuda_debug_set_wait_cycles(-1) == capi.EINVAL
+    assert L.qcs_cuda_debug_set_wait_cycles(1000) == capi.OK
+    assert L.qcs_cuda_debug_set_wait_cycles(0) == capi.OK  # back to the default
+
+
 def _replay(n, gates, order):
     ops = gates.ops()[order]
     g = W.GateList()
