@@ -775,6 +775,18 @@ def run_batch(args, dist):
             z, samples, ms = b.run()
             times.append(ms)
         ms = dist.max(float(np.mean(times)))
+        traffic = b.traffic()
+    peaks = measured_peaks()
+    achieved = traffic / (ms / 1e3) / 1e9
+    n_slot = sum(1 for n, _ in mine if n > tune["tile_q"])
+    roof = {"bound": "hbm", "kernel": "batch", "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+            "algorithmic_bytes_per_run": traffic,
+            "bytes_definition": "per instance above the tile (global slot): one write of its "
+                                "state in the first stage, a read and a write per later stage, "
+                                "one read for <Z0> and the sampling masses; plus the results",
+            "instances_in_global_slots": n_slot,
+            "instances_in_shared_memory": len(mine) - n_slot}
     check = None
     if dist.rank == 0 and not args.no_parity:
         O.build()
@@ -792,7 +804,7 @@ def run_batch(args, dist):
     line = {"mode": "batch", "instances": args.instances, "shots": args.shots,
             "n_gpus": dist.world, "ms_per_batch": ms,
             "instances_per_s": args.instances / (ms / 1e3),
-            "gate_apps_per_s": total_gates / (ms / 1e3), "schedule": tune,
+            "gate_apps_per_s": total_gates / (ms / 1e3), "schedule": tune, "roofline": roof,
             "check": check, "scaling": "strong" if dist.world > 1 else None}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)

@@ -259,6 +259,13 @@ int qcs_cuda_batch_schedule(qcs_cuda_batch *b, int *schedule);
 /* Instances above split_q qubits (and above the tile) are shared by
  * 2^(n - split_q) CTAs, at most half the grid; 27 never splits. */
 int qcs_cuda_batch_split(qcs_cuda_batch *b, int split_q);
+/* Algorithmic HBM bytes of one run under the schedule in force: for every
+ * instance above the tile (kept in a global slot), one write of its 2^n
+ * complex64 amplitudes in the first stage, a read and a write in each later
+ * stage, and one read for <Z_0> and the sampling masses; plus the results
+ * (8 bytes per instance and 8 per shot).  Instances that fit the tile live
+ * in shared memory and move no state bytes. */
+int qcs_cuda_batch_traffic(qcs_cuda_batch *b, double *hbm_bytes);
 /* Sets one schedule explicitly (split_q is kept). */
 int qcs_cuda_batch_config(qcs_cuda_batch *b, int threads, int tile_q,
                           int ctas_per_sm, int order);

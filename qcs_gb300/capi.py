@@ -115,6 +115,7 @@ def _declare(L):
         "qcs_cuda_batch_config": (i, [vp, i, i, i, i]),
         "qcs_cuda_batch_schedule": (i, [vp, ip]),
         "qcs_cuda_batch_split": (i, [vp, i]),
+        "qcs_cuda_batch_traffic": (i, [vp, dp]),
         "qcs_cuda_costmodel_create": (i, [i, C.c_ulonglong, vpp]),
         "qcs_cuda_costmodel_destroy": (i, [vp]),
         "qcs_cuda_costmodel_num_params": (i, [vp, ip]),
@@ -423,6 +424,12 @@ class Batch:
 
     def config(self, threads: int, tile_q: int, ctas_per_sm: int, order: int = 0):
         _check(lib().qcs_cuda_batch_config(self._h, threads, tile_q, ctas_per_sm, order))
+
+    def traffic(self) -> float:
+        """Algorithmic HBM bytes of one run (qcs_cuda_batch_traffic)."""
+        out = C.c_double()
+        _check(lib().qcs_cuda_batch_traffic(self._h, C.byref(out)))
+        return out.value
 
     def split(self, split_q: int):
         _check(lib().qcs_cuda_batch_split(self._h, split_q))

@@ -974,6 +974,16 @@ int qcs_cuda_batch_set_angles(qcs_cuda_batch *b, const double *angles) {
   return QCS_CUDA_OK;
 }
 
+int qcs_cuda_batch_traffic(qcs_cuda_batch *b, double *hbm_bytes) {
+  if (!b || !hbm_bytes) return set_error(QCS_CUDA_EINVAL, "null batch argument");
+  double bytes = 8.0 * b->count * (1.0 + b->shots);
+  for (const BInst &I : b->insts)
+    if (I.n > b->planned_tile_q)  // 2 nstages - 1 stage passes, 1 read-out pass
+      bytes += ldexp(8.0, I.n) * (2.0 * I.nstages);
+  *hbm_bytes = bytes;
+  return QCS_CUDA_OK;
+}
+
 int qcs_cuda_batch_run(qcs_cuda_batch *b, double *expect_z0, long long *samples, double *ms) {
   if (!b) return set_error(QCS_CUDA_EINVAL, "null batch");
   float t = 0.f;

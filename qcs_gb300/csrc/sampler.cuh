@@ -25,10 +25,12 @@ __device__ __forceinline__ double smp_prob(C x) {
   return ((double)x.x * (double)x.x) + ((double)x.y * (double)x.y);
 }
 
-// A thread's share of a full tile's probability mass: complex64 as 8 float4
-// loads issued together (units t, t + 256, ... of the tile's 2048 pairs of
-// amplitudes), |a|^2 summed in FP32 in that order and returned in FP64;
-// complex128 as 16 double2 loads, FP64 throughout.
+// A warp's share of a full tile's probability mass.  complex64: each thread
+// issues its 8 float4 loads together (units t, t + 256, ... of the tile's
+// 2048 pairs of amplitudes) and sums |a|^2 in FP32 in that order; the warp
+// adds its 32 partials by an FP32 tree (five roundings) and returns the sum
+// in FP64 -- GB300's FP64 rate would otherwise bound this pass.  complex128:
+// 16 double2 loads a thread, FP64 throughout.  Every lane returns the sum.
 template <typename C>
 __device__ __forceinline__ double smp_full_tile_mass(const C *v, i64 first);
 template <>
@@ -44,6 +46,8 @@ __device__ __forceinline__ double smp_full_tile_mass<float2>(const float2 *v, i6
     a = fmaf(x[k].x, x[k].x, fmaf(x[k].y, x[k].y, a));
     a = fmaf(x[k].z, x[k].z, fmaf(x[k].w, x[k].w, a));
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   return (double)a;
 }
 template <>
@@ -56,10 +60,11 @@ __device__ __forceinline__ double smp_full_tile_mass<double2>(const double2 *v, 
   double a = 0.0;
 #pragma unroll
   for (int k = 0; k < U; k++) a += smp_prob(x[k]);
-  return a;
+  return smp_warp_sum(a);
 }
 
-// The same for a state smaller than one full tile (its single tile).
+// The same for a state smaller than one full tile (its single tile); each
+// lane returns its own partial (the caller sums the warp in FP64).
 template <typename C>
 __device__ __forceinline__ double smp_small_tile_mass(const C *v, i64 tile) {
   double a = 0.0;
@@ -83,9 +88,8 @@ __global__ void __launch_bounds__(kSampleThreads)
     k_smp_tile_sums(const C *v, i64 tile, i64 n_tiles, double *sums) {
   __shared__ double part[kSampleThreads / 32];
   for (i64 t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-    double a = tile == kSampleTile ? smp_full_tile_mass<C>(v, t * kSampleTile)
-                                   : smp_small_tile_mass<C>(v, tile);
-    a = smp_warp_sum(a);
+    const double a = tile == kSampleTile ? smp_full_tile_mass<C>(v, t * kSampleTile)
+                                         : smp_warp_sum(smp_small_tile_mass<C>(v, tile));
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = a;
     __syncthreads();
     if (threadIdx.x < 32) {
