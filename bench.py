@@ -67,6 +67,9 @@ def parse():
                          "variational instances in one persistent launch; shards: launch "
                          "check, every rank reports its share of the batch (no GPU work)")
     ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--max-qubits", type=int, default=22,
+                    help="batch: largest instance (qubit counts uniform in [10, this]); "
+                         "smaller values give small profiling cases")
     ap.add_argument("--no-autotune", action="store_true",
                     help="batch: keep the default schedule (512 threads, tile 2^13, 2 CTAs/SM)")
     ap.add_argument("--shots", type=int, default=1024)
@@ -763,7 +766,7 @@ def run_batch(args, dist):
     from qcs_gb300 import capi
     from qcs_gb300 import workloads as W
     B.build()
-    inst = W.variational_batch(args.instances, args.seed)
+    inst = W.variational_batch(args.instances, args.seed, n_range=(10, args.max_qubits))
     mine = shard(inst, dist)
     with capi.Batch(mine, shots=args.shots, seed=args.seed) as b:
         tune = b.autotune(repeats=1) if not args.no_autotune else b.schedule()
