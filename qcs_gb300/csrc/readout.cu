@@ -90,8 +90,15 @@ __global__ void __launch_bounds__(kReduceThreads)
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       i64 i0 = 2 * (u + k * nthr);
-      accum<OP>(i0, x[k].x, x[k].y, q, pa, pb);
-      accum<OP>(i0 + 1, x[k].z, x[k].w, q, pa, pb);
+      if (OP == OP_MASK && q > 0) {
+        // both amplitudes of the unit share bit q: one selection per unit
+        const float p = (x[k].x * x[k].x + x[k].y * x[k].y) + (x[k].z * x[k].z + x[k].w * x[k].w);
+        if ((i0 >> q) & 1) pb += p;
+        else pa += p;
+      } else {
+        accum<OP>(i0, x[k].x, x[k].y, q, pa, pb);
+        accum<OP>(i0 + 1, x[k].z, x[k].w, q, pa, pb);
+      }
     }
     A += (double)pa;
     B += (double)pb;

@@ -101,48 +101,76 @@ __global__ void __launch_bounds__(kSampleThreads)
   }
 }
 
-// In-place exclusive prefix of x[0 .. n) (one block of 1024 threads, FP64,
-// fixed order: each thread a contiguous segment, then the segment totals);
-// the total goes to x[n].
+// In-place exclusive prefix of x[0 .. n) in FP64, the total into x[n]: one
+// block of 1024 threads walks x in chunks of 8192 entries with a running
+// carry.  Thread t owns the 8 adjacent entries 8t .. 8t+7 of a chunk (moved
+// in 16-byte pieces, so a warp reads and writes 2 KB contiguous); the
+// block scans the threads' totals (warp shuffles, then the 32 warp totals),
+// and each thread adds its entries one after another to its offset.  The
+// order of the additions is fixed, so the prefix is deterministic.
 __global__ void __launch_bounds__(1024) k_smp_prefix(double *x, i64 n) {
-  __shared__ double seg[1024];
-  const i64 per = (n + blockDim.x - 1) / blockDim.x;
-  const i64 b = threadIdx.x * per;
-  const i64 e = b + per < n ? b + per : n;
-  constexpr int B = 8;  // loads in flight per thread
-  double s = 0.0;
-  for (i64 i0 = b; i0 < e; i0 += B) {
-    double t[B];
+  constexpr int E = 8;
+  __shared__ double wtot[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  double carry = 0.0;
+  for (i64 c0 = 0; c0 < n; c0 += (i64)blockDim.x * E) {
+    const i64 i0 = c0 + (i64)t * E;
+    double v[E];
+    if (i0 + E <= n) {
+      const double2 *p = reinterpret_cast<const double2 *>(x + i0);
 #pragma unroll
-    for (int k = 0; k < B; k++) t[k] = i0 + k < e ? x[i0 + k] : 0.0;
-#pragma unroll
-    for (int k = 0; k < B; k++)
-      if (i0 + k < e) s += t[k];
-  }
-  seg[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double run = 0.0;
-    for (int k = 0; k < (int)blockDim.x; k++) {
-      const double t = seg[k];
-      seg[k] = run;
-      run += t;
-    }
-    x[n] = run;
-  }
-  __syncthreads();
-  double run = seg[threadIdx.x];
-  for (i64 i0 = b; i0 < e; i0 += B) {
-    double t[B];
-#pragma unroll
-    for (int k = 0; k < B; k++) t[k] = i0 + k < e ? x[i0 + k] : 0.0;
-#pragma unroll
-    for (int k = 0; k < B; k++)
-      if (i0 + k < e) {
-        x[i0 + k] = run;
-        run += t[k];
+      for (int k = 0; k < E / 2; k++) {
+        const double2 d = p[k];
+        v[2 * k] = d.x;
+        v[2 * k + 1] = d.y;
       }
+    } else {
+#pragma unroll
+      for (int k = 0; k < E; k++) v[k] = i0 + k < n ? x[i0 + k] : 0.0;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < E; k++) s += v[k];
+    double incl = s;  // inclusive scan of the thread totals within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = 0.0;
+    if (lane == 31) wtot[w] = incl;
+    __syncthreads();
+    if (w == 0) {  // inclusive scan of the warp totals
+      double wt = lane < (int)(blockDim.x >> 5) ? wtot[lane] : 0.0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, wt, o);
+        if (lane >= o) wt += y;
+      }
+      wtot[lane] = wt;
+    }
+    __syncthreads();
+    double run = carry + ((w > 0 ? wtot[w - 1] : 0.0) + excl);
+    double out[E];
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+      out[k] = run;
+      run += v[k];
+    }
+    if (i0 + E <= n) {
+      double2 *p = reinterpret_cast<double2 *>(x + i0);
+#pragma unroll
+      for (int k = 0; k < E / 2; k++) p[k] = make_double2(out[2 * k], out[2 * k + 1]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < E; k++)
+        if (i0 + k < n) x[i0 + k] = out[k];
+    }
+    carry += wtot[31];
+    __syncthreads();  // wtot is rewritten by the next chunk
   }
+  if (t == 0) x[n] = carry;
 }
 
 // One warp per draw r: the tile whose inclusive prefix first exceeds r (a
