@@ -368,7 +368,7 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
  * below the total).  Work is queued on `stream` (a cudaStream_t, NULL for the
  * default stream); the call does not wait for it.
  * Limit: count must be a power of two no larger than 2^28 amplitudes; the
- * scratch is a fixed 512 KB array inside the library, held on every GPU that
+ * scratch is a fixed array of about 544 KB inside the library, held on every GPU that
  * loads it until the process exits.  The first call on a device looks up
  * that array's device address and should come before any stream capture;
  * a device reset invalidates it (a call whose launch fails looks it up

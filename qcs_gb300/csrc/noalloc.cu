@@ -9,10 +9,11 @@
 // array that is part of the library image instead.
 //
 // The scratch is the per-tile probability prefix of the sampler: one double
-// per tile of 4096 amplitudes plus the total.  It lives in a file-scope
-// __device__ array sized for kNoAllocMaxTiles tiles (512 KB + 8 B), which
-// every GPU that loads the library holds until the process exits.  States
-// larger than kNoAllocMaxTiles * 4096 = 2^28 amplitudes are rejected.
+// per tile of 4096 amplitudes, then one per range of tiles (at most
+// kNoAllocMaxRanges) and the total.  It lives in a file-scope __device__
+// array of kNoAllocMaxTiles + kNoAllocMaxRanges + 1 doubles (about 544 KB),
+// which every GPU that loads the library holds until the process exits.
+// States larger than kNoAllocMaxTiles * 4096 = 2^28 amplitudes are rejected.
 //
 // Host code cannot use the array's name as a device address, so the device
 // address is looked up with cudaGetSymbolAddress once per device, with that
@@ -34,8 +35,9 @@ namespace qcs {
 
 constexpr i64 kNoAllocTile = kSampleTile;
 constexpr i64 kNoAllocMaxTiles = 65536;
+constexpr int kNoAllocMaxRanges = 4096;
 
-static __device__ __align__(256) double g_noalloc_prefix[kNoAllocMaxTiles + 1];
+static __device__ __align__(256) double g_noalloc_prefix[kNoAllocMaxTiles + kNoAllocMaxRanges + 1];
 
 static std::mutex g_noalloc_mu;
 static double *g_noalloc_addr[64];
@@ -81,16 +83,20 @@ static int na_launch(const C *v, i64 count, const double *draws, int shots, i64 
     rc = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
                     "cudaDeviceGetAttribute(multiprocessor count)");
   if (rc) return rc;
-  const int gt = (int)(n_tiles < (i64)sms * 8 ? n_tiles : (i64)sms * 8);
-  k_smp_tile_sums<C><<<gt, kSampleThreads, 0, st>>>(v, tile, n_tiles, prefix);
+  int G = 1;
+  i64 per = 1;
+  smp_ranges(n_tiles, sms, kNoAllocMaxRanges, &G, &per);
+  double *in = prefix, *boff = prefix + n_tiles;
+  k_smp_tile_sums<C><<<G, kSampleThreads, 0, st>>>(v, tile, n_tiles, per, in, boff);
   rc = check_launch("sample_noalloc tile sums");
   if (rc) return rc;
-  k_smp_prefix<<<1, 1024, 0, st>>>(prefix, n_tiles);
+  k_smp_prefix<<<1, 1024, 0, st>>>(boff, G);
   rc = check_launch("sample_noalloc prefix");
   if (rc || shots == 0) return rc;
   int blocks = (int)(((i64)shots * 32 + 255) / 256);
   if (blocks > sms * 16) blocks = sms * 16;
-  k_smp_sample<C><<<blocks, 256, 0, st>>>(v, tile, n_tiles, prefix, draws, shots, samples);
+  k_smp_sample<C><<<blocks, 256, 0, st>>>(v, tile, n_tiles, per, in, boff, G, draws, shots,
+                                         samples);
   return check_launch("sample_noalloc");
 }
 

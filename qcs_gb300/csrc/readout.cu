@@ -641,20 +641,23 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
   if (rc) return rc;
   const i64 tile = s->size / s->n_tiles;
   const DeviceInfo &d = s->dev;
-  int gt = s->n_tiles < (i64)d.num_sms * 8 ? (int)s->n_tiles : d.num_sms * 8;
+  int G = 1;
+  i64 per = 1;
+  smp_ranges(s->n_tiles, d.num_sms, d.num_sms * 8, &G, &per);
+  double *in = s->d_tile_prefix, *boff = s->d_tile_prefix + s->n_tiles;
   const double sb = s->prec == QCS_CUDA_C128 ? 16 : 8;
   prof_begin(s);
   if (s->prec == QCS_CUDA_C128)
-    k_smp_tile_sums<double2><<<gt, kSampleThreads, 0, s->stream>>>(
-        (const double2 *)s->vec, tile, s->n_tiles, s->d_tile_prefix);
+    k_smp_tile_sums<double2><<<G, kSampleThreads, 0, s->stream>>>(
+        (const double2 *)s->vec, tile, s->n_tiles, per, in, boff);
   else
-    k_smp_tile_sums<float2><<<gt, kSampleThreads, 0, s->stream>>>(
-        (const float2 *)s->vec, tile, s->n_tiles, s->d_tile_prefix);
+    k_smp_tile_sums<float2><<<G, kSampleThreads, 0, s->stream>>>(
+        (const float2 *)s->vec, tile, s->n_tiles, per, in, boff);
   rc = launched(s, KC_SAMPLE, s->size * sb, "sample tile sums");
   if (rc) return rc;
   prof_begin(s);
-  k_smp_prefix<<<1, 1024, 0, s->stream>>>(s->d_tile_prefix, s->n_tiles);
-  rc = launched(s, KC_SAMPLE, 16.0 * s->n_tiles, "sample prefix");
+  k_smp_prefix<<<1, 1024, 0, s->stream>>>(boff, G);
+  rc = launched(s, KC_SAMPLE, 16.0 * G, "sample prefix");
   if (rc) return rc;
   memcpy(s->h_draws, random_vals, (size_t)shots * sizeof(double));
   rc = copy_h2d(s, s->d_draws, s->h_draws, (size_t)shots * sizeof(double), "sample draws upload");
@@ -665,11 +668,11 @@ int qcs_cuda_sample(qcs_cuda_state *s, const double *random_vals, int shots,
   prof_begin(s);
   if (s->prec == QCS_CUDA_C128)
     k_smp_sample<double2><<<blocks, threads, 0, s->stream>>>(
-        (const double2 *)s->vec, tile, s->n_tiles, s->d_tile_prefix, s->d_draws, shots,
+        (const double2 *)s->vec, tile, s->n_tiles, per, in, boff, G, s->d_draws, shots,
         s->d_samples);
   else
     k_smp_sample<float2><<<blocks, threads, 0, s->stream>>>(
-        (const float2 *)s->vec, tile, s->n_tiles, s->d_tile_prefix, s->d_draws, shots,
+        (const float2 *)s->vec, tile, s->n_tiles, per, in, boff, G, s->d_draws, shots,
         s->d_samples);
   rc = launched(s, KC_SAMPLE, (double)shots * tile * sb, "sample");
   if (!rc) rc = copy_d2h(s, s->h_samples, s->d_samples, (size_t)shots * sizeof(i64),

@@ -1,5 +1,13 @@
 // sampler.cuh -- the kernels of shot sampling (qc_run_shots, src/qcs.c:575-607):
 // per-tile probability masses, their exclusive prefix, and one warp per draw.
+//
+// Scratch layout (doubles): in[0 .. n_tiles) then boff[0 .. G].  The tiles
+// are cut into G contiguous ranges of `per` tiles, one per block of the
+// tile-sum pass; in[t] is the exclusive prefix of tile t within its range and
+// boff[b] the exclusive prefix of the range totals, boff[G] the total mass.
+// The prefix of tile t is boff[t / per] + in[t].  Summing within ranges on
+// many SMs keeps the FP64 additions off a single SM (GB300's FP64 rate per
+// SM is low).
 // Shared by qcs_cuda_sample (per-state scratch) and qcs_cuda_sample_noalloc
 // (a fixed library array), so that both give the same indices for the same
 // draws.  The kernels have internal linkage: each translation unit that
@@ -13,6 +21,17 @@ namespace {
 
 constexpr i64 kSampleTile = 4096;    // amplitudes per tile of the prefix
 constexpr int kSampleThreads = 256;  // threads of the tile-sum blocks
+
+// The ranges of the tile-sum pass: G blocks of `per` tiles (at most
+// max_blocks blocks, 8 per SM).
+inline void smp_ranges(i64 n_tiles, int sms, int max_blocks, int *G, i64 *per) {
+  i64 g = (i64)sms * 8;
+  if (g > max_blocks) g = max_blocks;
+  if (g > n_tiles) g = n_tiles;
+  if (g < 1) g = 1;
+  *per = (n_tiles + g - 1) / g;
+  *G = (int)((n_tiles + *per - 1) / *per);
+}
 
 __device__ __forceinline__ double smp_warp_sum(double x) {
 #pragma unroll
@@ -81,13 +100,17 @@ __device__ __forceinline__ double smp_small_tile_mass<float2>(const float2 *v, i
   return (double)a;
 }
 
-// Probability mass of each tile into sums[0 .. n_tiles): one block per tile
-// at a time, FP64 across the block's threads in a fixed order.
+// Tile masses: block b takes tiles [b per, (b + 1) per) one after another
+// (FP64 across its threads in a fixed order), writes each tile's exclusive
+// prefix within the range to in[t] and the range total to bsum[b].
 template <typename C>
 __global__ void __launch_bounds__(kSampleThreads)
-    k_smp_tile_sums(const C *v, i64 tile, i64 n_tiles, double *sums) {
+    k_smp_tile_sums(const C *v, i64 tile, i64 n_tiles, i64 per, double *in, double *bsum) {
   __shared__ double part[kSampleThreads / 32];
-  for (i64 t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+  const i64 t0 = (i64)blockIdx.x * per;
+  const i64 t1 = t0 + per < n_tiles ? t0 + per : n_tiles;
+  double run = 0.0;  // thread 0: the range's running total
+  for (i64 t = t0; t < t1; t++) {
     const double a = tile == kSampleTile ? smp_full_tile_mass<C>(v, t * kSampleTile)
                                          : smp_warp_sum(smp_small_tile_mass<C>(v, tile));
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = a;
@@ -95,13 +118,18 @@ __global__ void __launch_bounds__(kSampleThreads)
     if (threadIdx.x < 32) {
       double b = threadIdx.x < kSampleThreads / 32 ? part[threadIdx.x] : 0.0;
       b = smp_warp_sum(b);
-      if (threadIdx.x == 0) sums[t] = b;
+      if (threadIdx.x == 0) {
+        in[t] = run;
+        run += b;
+      }
     }
     __syncthreads();
   }
+  if (threadIdx.x == 0) bsum[blockIdx.x] = run;
 }
 
-// In-place exclusive prefix of x[0 .. n) in FP64, the total into x[n]: one
+// In-place exclusive prefix of x[0 .. n) in FP64, the total into x[n] (the
+// range totals bsum[0 .. G) into the offsets boff[0 .. G]): one
 // block of 1024 threads walks x in chunks of 8192 entries with a running
 // carry.  Thread t owns the 8 adjacent entries 8t .. 8t+7 of a chunk (moved
 // in 16-byte pieces, so a warp reads and writes 2 KB contiguous); the
@@ -174,40 +202,51 @@ __global__ void __launch_bounds__(1024) k_smp_prefix(double *x, i64 n) {
 }
 
 // One warp per draw r: the tile whose inclusive prefix first exceeds r (a
-// binary search), then an FP64 scan of that tile 32 amplitudes at a time
-// (four groups' loads in flight together).  Result: the first index with
+// binary search over the range offsets, then one over the tiles of that
+// range), then an FP64 scan of that tile 32 amplitudes at a time (four
+// groups' loads in flight together).  Result: the first index with
 // r < running sum (strict, as src/qcs.c:600), or -1 when r is not below the
 // total.  When r falls in a tile by its total but not by the element scan
 // (rounding at the tile's upper edge), the tile's last nonzero index.
 template <typename C>
-__global__ void k_smp_sample(const C *v, i64 tile, i64 n_tiles, const double *prefix,
-                             const double *draws, int shots, i64 *out) {
-  constexpr int G = 4;  // 32-amplitude groups loaded together
+__global__ void k_smp_sample(const C *v, i64 tile, i64 n_tiles, i64 per, const double *in,
+                             const double *boff, int G, const double *draws, int shots, i64 *out) {
+  constexpr int G4 = 4;  // 32-amplitude groups loaded together
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int s = warp; s < shots; s += nwarps) {
     const double r = draws[s];
     i64 result = -1;
-    if (r < prefix[n_tiles]) {
-      i64 lo = 0, hi = n_tiles - 1;  // smallest t with r < prefix[t + 1]
+    if (r < boff[G]) {
+      int blo = 0, bhi = G - 1;  // the range: smallest b with r < boff[b + 1]
+      while (blo < bhi) {
+        const int mid = (blo + bhi) >> 1;
+        if (r < boff[mid + 1]) bhi = mid;
+        else blo = mid + 1;
+      }
+      const double off = boff[blo], end_off = boff[blo + 1];
+      const i64 t0 = (i64)blo * per;
+      const i64 t1 = t0 + per < n_tiles ? t0 + per : n_tiles;
+      i64 lo = t0, hi = t1 - 1;  // the tile: smallest t with r < prefix(t + 1)
       while (lo < hi) {
         const i64 mid = (lo + hi) >> 1;
-        if (r < prefix[mid + 1]) hi = mid;
+        const double next = mid + 1 < t1 ? off + in[mid + 1] : end_off;
+        if (r < next) hi = mid;
         else lo = mid + 1;
       }
-      double cum = prefix[lo];
+      double cum = off + in[lo];
       i64 last_nonzero = lo * tile;
       const i64 end = (lo + 1) * tile;
-      for (i64 base = lo * tile; base < end && result < 0; base += 32 * G) {
-        double p[G];
+      for (i64 base = lo * tile; base < end && result < 0; base += 32 * G4) {
+        double p[G4];
 #pragma unroll
-        for (int k = 0; k < G; k++) {
+        for (int k = 0; k < G4; k++) {
           const i64 i = base + 32 * k + lane;
           p[k] = i < end ? smp_prob(v[i]) : 0.0;
         }
 #pragma unroll
-        for (int k = 0; k < G; k++) {
+        for (int k = 0; k < G4; k++) {
           const i64 gb = base + 32 * k;
           if (result >= 0 || gb >= end) break;  // warp-uniform
           double incl = p[k];

@@ -226,7 +226,10 @@ int ensure_sample_scratch(qcs_cuda_state *s, int shots) {
   if (!s->d_tile_prefix) {
     i64 tile = s->size < 4096 ? s->size : 4096;
     s->n_tiles = s->size / tile;
-    rc = dmalloc((void **)&s->d_tile_prefix, (size_t)(s->n_tiles + 1) * sizeof(double),
+    // the tiles' prefixes within their ranges, then the range offsets and
+    // the total (at most 8 ranges per SM)
+    rc = dmalloc((void **)&s->d_tile_prefix,
+                 (size_t)(s->n_tiles + (i64)s->dev.num_sms * 8 + 1) * sizeof(double),
                  "cudaMalloc(tile prefix)");
     if (rc) return rc;
   }
