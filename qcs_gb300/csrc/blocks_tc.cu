@@ -375,12 +375,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (p < g.nruns && it + g.pf_ahead < w.count)  // nruns <= 128 < 256 producers
         prefetch_l2(v + tile_base(w.at(it + g.pf_ahead), g) + g.run_off[p],
                     (uint32_t)g.run_bytes);
-      // every lane of a warp takes the same decision (the low-mode norm
-      // exchange below is a full-warp shuffle)
-      if (it >= 2 &&
-          !__all_sync(0xffffffffu, wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err,
-                                            1, wait)))
-        break;
+      // in low mode every lane of a warp takes the same decision: the norm
+      // exchange below is a full-warp shuffle
+      if (it >= 2) {
+        bool ok = wait_bar(bar(2 + stage), ((it - 2) >> 1) & 1, abort_flag, err, 1, wait);
+        if (MODE == kLowMode) ok = __all_sync(0xffffffffu, ok);
+        if (!ok) break;
+      }
       uint8_t *ahi = sA + (2 * stage) * S::A_BYTES;
       uint8_t *alo = ahi + S::A_BYTES;
       float *sq = colsq + (it % kSqSlots) * 2 * kTcM;
@@ -818,9 +819,11 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
         prefetch_l2(v + tile_base(w.at(it + g.pf_ahead), g) + g.run_off[p],
                     (uint32_t)g.run_bytes);
       // stage b is free once the MMAs of chunk q - 2 are done
-      if (q >= 2 && !__all_sync(0xffffffffu, wait_bar(bar(2 + b), (uint32_t)(((q - 2) >> 1) & 1),
-                                                       abort_flag, err, 1, wait)))
-        return false;
+      if (q >= 2) {
+        bool ok = wait_bar(bar(2 + b), (uint32_t)(((q - 2) >> 1) & 1), abort_flag, err, 1, wait);
+        if (MODE == kLowMode) ok = __all_sync(0xffffffffu, ok);  // low-mode norm shuffles
+        if (!ok) return false;
+      }
       if (c == 0) {
         part = 0.f;
 #pragma unroll
