@@ -247,7 +247,7 @@ int qcs_cuda_batch_set_angles(qcs_cuda_batch *b, const double *angles);
 int qcs_cuda_batch_run(qcs_cuda_batch *b, double *expect_z0,
                        long long *samples, double *ms);
 /* Times every schedule (threads per CTA 256/512/1024, tile 2^12..2^14,
- * 1 or 2 CTAs per SM, largest-first or given order) on this batch, then how
+ * 1, 2 or 4 CTAs per SM as fit, largest-first or given order) on this batch, then how
  * widely large instances spread (an instance above split_q qubits is shared
  * by 2^(n - split_q) CTAs, split_q in 17..20 or never), and keeps the
  * fastest; chosen (4 ints) receives threads, tile qubits, CTAs per SM and

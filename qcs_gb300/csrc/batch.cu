@@ -82,7 +82,7 @@ struct BGate {
 struct BatchTune {
   int threads;      // 256, 512 or 1024
   int tile_q;       // 12, 13 or 14
-  int ctas_per_sm;  // 1 or 2
+  int ctas_per_sm;  // 1, 2 or 4 (as many as shared memory and registers allow)
   int order;        // 0: largest first, 1: given order
   int split_q;      // instances above split_q qubits run on 2^(n - split_q) CTAs
 };
@@ -1015,15 +1015,16 @@ int qcs_cuda_batch_autotune(qcs_cuda_batch *b, int repeats, int *chosen) {
   };
   const int threads[] = {256, 512, 1024};
   const int tiles[] = {12, 13, 14};
-  const int ctas[] = {1, 2};
+  const int ctas[] = {1, 2, 4};
   BatchTune best = b->tune;
   float best_ms = 1e30f;
   for (int th : threads)
     for (int tq : tiles)
       for (int cp : ctas)
         for (int ord = 0; ord < 2; ord++) {
-          // two CTAs per SM must fit in shared memory
-          if (cp == 2 && smem_for(tq) * 2 > 220 * 1024) continue;
+          // the CTAs of an SM must fit its shared memory, and four only
+          // with 256 threads (64 registers a thread)
+          if (smem_for(tq) * cp > 220 * 1024 || th * cp > 1024) continue;
           BatchTune t = b->tune;
           t.threads = th;
           t.tile_q = tq;
@@ -1085,10 +1086,12 @@ int qcs_cuda_batch_config(qcs_cuda_batch *b, int threads, int tile_q, int ctas_p
                           int order) {
   if (!b) return set_error(QCS_CUDA_EINVAL, "null batch");
   if ((threads != 256 && threads != 512 && threads != 1024) || tile_q < 10 || tile_q > 14 ||
-      ctas_per_sm < 1 || ctas_per_sm > 2 || order < 0 || order > 1)
+      ctas_per_sm < 1 || ctas_per_sm > 4 || ctas_per_sm == 3 || order < 0 || order > 1 ||
+      threads * ctas_per_sm > 1024)
     return set_error(QCS_CUDA_EINVAL, "bad batch schedule");
-  if (ctas_per_sm == 2 && smem_for(tile_q) * 2 > 220 * 1024)
-    return set_error(QCS_CUDA_EINVAL, "two CTAs of tile 2^%d do not fit one SM", tile_q);
+  if (smem_for(tile_q) * ctas_per_sm > 220 * 1024)
+    return set_error(QCS_CUDA_EINVAL, "%d CTAs of tile 2^%d do not fit one SM", ctas_per_sm,
+                     tile_q);
   BatchTune t = b->tune;
   t.threads = threads;
   t.tile_q = tile_q;

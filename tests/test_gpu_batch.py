@@ -47,7 +47,7 @@ def oracle_instance(n, g):
         return o.expect_z(0), np.abs(o.amplitudes()) ** 2
 
 
-@pytest.mark.parametrize("schedule", [None, (256, 12, 2, 1), (1024, 14, 1, 0)])
+@pytest.mark.parametrize("schedule", [None, (256, 12, 2, 1), (1024, 14, 1, 0), (256, 12, 4, 0)])
 def test_batch_matches_oracle(schedule):
     inst = W.variational_batch(48, seed=5, n_range=(6, 17), depth_range=(2, 8))
     with capi.Batch(inst, shots=2048, seed=9) as b:
