@@ -211,6 +211,47 @@ def test_sample_indices_vs_oracle(n):
         assert a[1] in (-1, b[1])
 
 
+def sample_rule(amps: np.ndarray, draws: np.ndarray) -> np.ndarray:
+    """qc_run_shots' rule (src/qcs.c:589-605) on FP64 amplitudes: the first
+    index whose sequential running sum of |a|^2 exceeds the draw, else -1
+    (np.cumsum adds in order, as the reference's loop does)."""
+    cum = np.cumsum(np.abs(amps.astype(np.complex128)) ** 2)
+    idx = np.searchsorted(cum, draws, side="right")
+    return np.where(idx < len(cum), idx, -1)
+
+
+@pytest.mark.parametrize("n", [23])
+def test_sample_indices_vs_oracle_several_tiles_per_range(n):
+    """2048 tiles of 4096 amplitudes: the tile-sum pass gives each block a
+    range of two tiles, so the prefix is a range offset plus a prefix within
+    the range, and each shot searches the ranges, then the tiles."""
+    _, g = W.random_circuit(n, 31, 60, with_qft=False)
+    draws = np.random.default_rng(n).random(3000)
+    draws[:2] = [0.0, 0.5]
+    with capi.State(n, capi.C128) as s, oracle_state(n, g) as o:
+        s.run(g)
+        a = s.sample(draws)
+        b = sample_rule(o.amplitudes(), draws)
+        # a draw within FP64 rounding of a tile edge may land on either side
+        assert np.mean(a == b) > 0.999, int(np.sum(a != b))
+        assert np.array_equal(a[:2], b[:2])
+
+
+def test_sample_c64_large_state_vs_oracle():
+    """complex64 at 24 qubits (4096 tiles, ranges of four): FP32 tile masses
+    move a range edge by ~1e-7 of a tile's mass, so almost every index
+    equals the FP64 oracle's."""
+    n = 24
+    g = W.brick_circuit(n, 2, 5)
+    draws = np.random.default_rng(7).random(4000)
+    with capi.State(n, capi.C64) as s, oracle_state(n, g) as o:
+        s.run(g)
+        a = s.sample(draws)
+        b = sample_rule(o.amplitudes(), draws)
+    assert np.mean(a == b) > 0.999, int(np.sum(a != b))
+    assert np.all(a >= 0)
+
+
 def test_normalize_rule():
     with capi.State(6, capi.C128) as s:
         v = np.zeros(64, complex)
