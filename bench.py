@@ -611,6 +611,38 @@ def run_sweeps(args, dist):
     print(json.dumps(line), flush=True)
 
 
+def fp64_ops_physical(gates, n: int) -> float:
+    """FP64 operations of a gate list's complex128 sweeps in PHYSICAL
+    semantics, counted per kernel: a complex product is 6 operations (4
+    multiplies, 2 adds, no FMA: the reference's order), a sum 2.  Dense 2x2
+    (H, RX, RY): 2 products + 1 sum per output, 28 per pair; exchange (X, Y,
+    CNOT): 1 product per output, 12 per pair; diagonal (RZ): 1 product per
+    amplitude; phase (Z, P, CPHASE): 1 product per touched amplitude."""
+    from qcs_gb300 import workloads as W
+    N = float(1 << n)
+    ops = 0.0
+    for k in gates.kinds:
+        k = int(k)
+        if k in (W.H, W.RX, W.RY):
+            ops += 28 * N / 2
+        elif k in (W.X, W.Y):
+            ops += 12 * N / 2
+        elif k == W.RZ:
+            ops += 6 * N
+        elif k in (W.Z, W.P):
+            ops += 6 * N / 2
+        elif k == W.CNOT:
+            ops += 12 * N / 4
+        elif k == W.CPHASE:
+            ops += 6 * N / 4
+    return ops
+
+
+# GB300's FP64 rate: 1.25 TFLOP/s counting a fused multiply-add as two; the
+# complex128 sweeps issue separate multiplies and adds, one per lane-cycle.
+FP64_NOMINAL_OPS = 0.625e12
+
+
 def run_random20(args, dist):
     """20 qubits, complex128, random basis state, QFT, 200 random gates, one
     kernel per gate.  REFERENCE semantics must equal the reference's
@@ -655,6 +687,16 @@ def run_random20(args, dist):
             o.run(full)
         cpu1_s = time.perf_counter() - t0
         O.set_threads(prev)
+        if name == "physical":
+            fops = fp64_ops_physical(full, n)
+            out["fp64_roofline"] = {
+                "bound": "fp64", "ops_per_circuit": fops,
+                "achieved_ops_per_s": fops / (ms / 1e3), "peak_ops_per_s": FP64_NOMINAL_OPS,
+                "frac": fops / (ms / 1e3) / FP64_NOMINAL_OPS,
+                "peak_source": "nominal (1.25 TFLOP/s with FMA counted as 2; not measured "
+                               "on this pool)",
+                "note": "the 16 MB (complex128) state stays in L2; the sweeps are bound by "
+                        "FP64 issue, plus one launch per gate"}
         out[name] = {"gate_apps_per_s": len(full) / (ms / 1e3), "ms_per_circuit": ms,
                      "bit_exact": bool(np.array_equal(a.view(np.float64), ref.view(np.float64))),
                      "max_abs_err": float(np.max(np.abs(a - ref))),

@@ -224,6 +224,39 @@ __global__ void __launch_bounds__(kSweepThreads)
   }
 }
 
+// Exchange gates, m = [[0, m01], [m10, 0]] (X, Y, and CNOT on its control=1
+// pairs), in place: v0' = m01 v1, v1' = m10 v0.  The dense formula's other
+// two products are +-0, so the values equal c_add(c_mul(g0,v0), c_mul(g1,v1))
+// (at most the sign of a zero differs) with a third of its operations: on a
+// complex128 state, whose sweeps GB300's FP64 rate bounds, that is the time.
+// CTRL: pairs with the control bit set, lo enumerated as in k_ctrl1q.
+template <typename C, bool CTRL>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_exch1q(C *v, i64 npairs, int blo, int bhi, i64 cmask, int t, C m01, C m10) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  const i64 tb = 1LL << t;
+  i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p < npairs; p += kUnroll * nthr) {
+    C v0[kUnroll], v1[kUnroll];
+    i64 lo[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      const i64 q = p + u * nthr;
+      lo[u] = CTRL ? (insert_zero(insert_zero(q, blo), bhi) | cmask) : insert_zero(q, t);
+      if (q < npairs) {
+        v0[u] = v[lo[u]];
+        v1[u] = v[lo[u] + tb];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      if (p + u * nthr >= npairs) continue;
+      v[lo[u]] = cmul(m01, v1[u]);
+      v[lo[u] + tb] = cmul(m10, v0[u]);
+    }
+  }
+}
+
 // The reference's controlled sweep (src/q_gates.c:277-297), out of place:
 // every pair is copied, except that control=1 pairs get
 // lo := c_add(c_mul(g0,v0), c_mul(g1,v1)) and keep hi := v1.
@@ -305,8 +338,12 @@ static int apply_1q_t(qcs_cuda_state *s, const double m[8], int t) {
   }
   i64 np = s->size / 2;
   prof_begin(s);
-  k_dense1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads, 0,
-                 s->stream>>>(v, v, np, t, g);
+  if (std::is_same<C, double2>::value && is_zero(m) && is_zero(m + 6))  // X, Y
+    k_exch1q<C, false><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
+                         kSweepThreads, 0, s->stream>>>(v, np, -1, -1, 0, t, g.g[1], g.g[2]);
+  else
+    k_dense1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads,
+                   0, s->stream>>>(v, v, np, t, g);
   return launched(s, KC_DENSE1Q, 2 * Ns, "apply_1q");
 }
 
@@ -353,6 +390,9 @@ static int apply_ctrl_t(qcs_cuda_state *s, const double m[8], int c, int t) {
   if (std::is_same<C, float2>::value && blo >= 1)
     k_ctrl1q_v2<<<grid_for(np / 2, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads,
                   0, s->stream>>>((float4 *)v, np / 2, blo, bhi, cmask, t, to_mat2<float2>(m));
+  else if (std::is_same<C, double2>::value && is_zero(m) && is_zero(m + 6))  // CNOT
+    k_exch1q<C, true><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM),
+                        kSweepThreads, 0, s->stream>>>(v, np, blo, bhi, cmask, t, g.g[1], g.g[2]);
   else
     k_ctrl1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads, 0,
                   s->stream>>>(v, np, blo, bhi, cmask, t, g);
