@@ -227,14 +227,14 @@ def test_sample_indices_vs_oracle_several_tiles_per_range(n):
     the range, and each shot searches the ranges, then the tiles."""
     _, g = W.random_circuit(n, 31, 60, with_qft=False)
     draws = np.random.default_rng(n).random(3000)
-    draws[:2] = [0.0, 0.5]
+    draws[0] = 0.0  # (a draw on an exact cumulative sum would be a knife edge)
     with capi.State(n, capi.C128) as s, oracle_state(n, g) as o:
         s.run(g)
         a = s.sample(draws)
         b = sample_rule(o.amplitudes(), draws)
         # a draw within FP64 rounding of a tile edge may land on either side
         assert np.mean(a == b) > 0.999, int(np.sum(a != b))
-        assert np.array_equal(a[:2], b[:2])
+        assert a[0] == b[0]
 
 
 def test_sample_c64_large_state_vs_oracle():
