@@ -237,17 +237,19 @@ def test_sample_indices_vs_oracle_several_tiles_per_range(n):
         assert a[0] == b[0]
 
 
-def test_sample_c64_large_state_vs_oracle():
-    """complex64 at 24 qubits (4096 tiles, ranges of four): FP32 tile masses
-    move a range edge by ~1e-7 of a tile's mass, so almost every index
-    equals the FP64 oracle's."""
+def test_sample_c64_large_state_vs_rule():
+    """complex64 at 24 qubits (4096 tiles, ranges of four), against the rule
+    applied in FP64 to the same amplitudes: the sampler's FP32 tile masses
+    move a tile edge by ~1e-7 of a tile's mass, so almost every index is the
+    rule's.  (Against the FP64 oracle's own state the indices would also
+    move with the complex64 circuit's ~1e-6 norm error.)"""
     n = 24
     g = W.brick_circuit(n, 2, 5)
     draws = np.random.default_rng(7).random(4000)
-    with capi.State(n, capi.C64) as s, oracle_state(n, g) as o:
+    with capi.State(n, capi.C64) as s:
         s.run(g)
         a = s.sample(draws)
-        b = sample_rule(o.amplitudes(), draws)
+        b = sample_rule(s.amplitudes(), draws)
     assert np.mean(a == b) > 0.999, int(np.sum(a != b))
     assert np.all(a >= 0)
 
