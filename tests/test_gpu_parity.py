@@ -239,10 +239,14 @@ def test_sample_indices_vs_oracle_several_tiles_per_range(n):
 
 def test_sample_c64_large_state_vs_rule():
     """complex64 at 24 qubits (4096 tiles, ranges of four), against the rule
-    applied in FP64 to the same amplitudes: the sampler's FP32 tile masses
-    move a tile edge by ~1e-7 of a tile's mass, so almost every index is the
-    rule's.  (Against the FP64 oracle's own state the indices would also
-    move with the complex64 circuit's ~1e-6 norm error.)"""
+    applied in FP64 to the same amplitudes.  The sampler sums a complex64
+    tile's |a|^2 in FP32 (per thread, then a warp tree) and in FP64 beyond:
+    a tile mass is off by ~5e-8 of itself, and over 4096 tiles the prefix
+    where a tile's scan starts by ~1e-9, a few percent of one amplitude's
+    probability (~6e-8) here.  So a draw occasionally lands one index over,
+    as it would with the state's own FP32 rounding; 99 % of the indices must
+    be the rule's.  (Against the FP64 oracle's own state the indices would
+    also move with the complex64 circuit's ~1e-6 norm error.)"""
     n = 24
     g = W.brick_circuit(n, 2, 5)
     draws = np.random.default_rng(7).random(4000)
@@ -250,7 +254,8 @@ def test_sample_c64_large_state_vs_rule():
         s.run(g)
         a = s.sample(draws)
         b = sample_rule(s.amplitudes(), draws)
-    assert np.mean(a == b) > 0.999, int(np.sum(a != b))
+    assert np.mean(a == b) > 0.99, int(np.sum(a != b))
+    assert np.all(np.abs(a - b) <= 64)  # never another region of the state
     assert np.all(a >= 0)
 
 
