@@ -337,9 +337,34 @@ struct PlanCache {
 // while their total stays under this many bytes.
 constexpr size_t kPlanCacheMatBytes = 64u << 20;
 
+// A plain run (one kernel per op) kept as a CUDA graph.  Small states run
+// circuits of short kernels whose launches, one per gate, take as long as
+// the kernels (a 20-qubit complex128 QFT phase: ~3 us of work).  The same op
+// list, byte for byte, is captured into a graph on its second run in a row
+// and replayed from then on: one graph launch per circuit.  PHYSICAL
+// semantics only (REFERENCE semantics swap the state's two buffers on the
+// host per gate).  The cached amplitude sum is reset before the capture and
+// before every replay, so the reductions the graph recorded are the ones a
+// fresh run would make.
+struct PlainGraph {
+  std::vector<qcs_cuda_op> ops;
+  int seen = 0;                   // runs of this op list in a row
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;         // kernels in the graph
+  int sum_valid_end = 0;          // the cached-sum flag after a run
+  ~PlainGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+constexpr int kPlainGraphMaxQubits = 26;  // above, a gate's kernel outlasts its launch
+constexpr int kPlainGraphMinOps = 16;
+
 void plan_cache_free(qcs_cuda_state *s) {
   delete s->plans;
   s->plans = nullptr;
+  delete s->plain_graph;
+  s->plain_graph = nullptr;
 }
 
 static bool plan_cache_hit(const PlanCache *c, const qcs_cuda_op *ops, int count, int n, int k,
@@ -445,16 +470,70 @@ static int execute_plan(qcs_cuda_state *s, const qcs_cuda_op *ops,
   return QCS_CUDA_OK;
 }
 
+static int run_plain(qcs_cuda_state *s, const qcs_cuda_op *ops, int count) {
+  for (int i = 0; i < count; i++) {
+    int rc = apply_op(s, ops[i]);
+    if (rc) return rc;
+  }
+  return QCS_CUDA_OK;
+}
+
+// The plain run through the kept graph (see PlainGraph).
+static int run_plain_kept(qcs_cuda_state *s, const qcs_cuda_op *ops, int count) {
+  PlainGraph *g = s->plain_graph;
+  const bool same = g && (int)g->ops.size() == count &&
+                    memcmp(g->ops.data(), ops, (size_t)count * sizeof(qcs_cuda_op)) == 0;
+  if (!same) {
+    delete g;
+    g = new PlainGraph();
+    g->ops.assign(ops, ops + count);
+    s->plain_graph = g;
+  }
+  g->seen++;
+  if (g->exec) {
+    invalidate_sum(s);
+    int rc = check_cuda(cudaGraphLaunch(g->exec, s->stream), "plain graph launch");
+    if (rc) return rc;
+    s->launches += g->launches;
+    s->sum_valid = g->sum_valid_end;
+    return QCS_CUDA_OK;
+  }
+  if (g->seen < 2) return run_plain(s, ops, count);
+  // second run in a row: record it, then launch the recording
+  invalidate_sum(s);
+  const long long l0 = s->launches;
+  int rc = check_cuda(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal),
+                      "plain graph capture");
+  if (rc) return rc;
+  rc = run_plain(s, ops, count);
+  cudaGraph_t graph = nullptr;
+  const int rc_end = check_cuda(cudaStreamEndCapture(s->stream, &graph), "plain graph capture end");
+  if (!rc) rc = rc_end;
+  if (!rc) rc = check_cuda(cudaGraphInstantiate(&g->exec, graph, 0), "plain graph instantiate");
+  if (graph) cudaGraphDestroy(graph);
+  if (rc) {
+    s->launches = l0;
+    g->exec = nullptr;
+    return rc;
+  }
+  g->launches = s->launches - l0;
+  g->sum_valid_end = s->sum_valid;
+  s->launches = l0 + g->launches;
+  invalidate_sum(s);
+  rc = check_cuda(cudaGraphLaunch(g->exec, s->stream), "plain graph launch");
+  if (!rc) s->sum_valid = g->sum_valid_end;
+  return rc;
+}
+
 int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda_run_options *opt) {
   int rc = validate_ops(s, ops, count);
   if (rc) return rc;
   int k = opt ? opt->fusion_k : 0;
   if (k <= 1 || s->sem == QCS_CUDA_REFERENCE) {
-    for (int i = 0; i < count; i++) {
-      rc = apply_op(s, ops[i]);
-      if (rc) return rc;
-    }
-    return QCS_CUDA_OK;
+    const bool keep = !(opt && (opt->flags & QCS_RUN_NO_PLAN_CACHE)) &&
+                      s->sem == QCS_CUDA_PHYSICAL && !s->prof &&
+                      s->n <= kPlainGraphMaxQubits && count >= kPlainGraphMinOps;
+    return keep ? run_plain_kept(s, ops, count) : run_plain(s, ops, count);
   }
   const int engine = opt->fusion_engine;
   k = fusion_cap(s, k, engine);

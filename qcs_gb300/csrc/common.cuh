@@ -53,6 +53,7 @@ enum KClass {
 struct ProfData;  // per-state event bookkeeping (state.cu)
 struct TcRing;    // tensor-core engine block-matrix uploads (blocks_tc.cu)
 struct PlanCache; // kept fused plan of the last run (blocks.cu)
+struct PlainGraph;  // kept plain run as a CUDA graph (blocks.cu)
 struct TcResident;  // a tensor-core block with its image on the device (blocks_tc.cu)
 // What a tensor-core block also does: take the state through a physical
 // diffusion first (the block reads psi, acts on 2m - psi), and/or leave the
@@ -103,6 +104,7 @@ struct qcs_cuda_state {
   int *d_err;             // device error flag (bounded waits that gave up)
   qcs_cuda_costmodel *cm; // model for QCS_PARTITION_LEARNED (not owned)
   qcs::PlanCache *plans;  // last fused run's plan and block matrices
+  qcs::PlainGraph *plain_graph;  // last plain run, captured once repeated
   // bytes moved between host and device on this state's behalf: explicit
   // copies and the matrices carried in kernel parameters
   long long h2d_bytes;

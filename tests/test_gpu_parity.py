@@ -99,6 +99,64 @@ def test_reference_semantics_controlled_rule(prec):
                 np.testing.assert_allclose(s.amplitudes(), o.amplitudes(), atol=1e-5)
 
 
+def test_plain_runs_replay_from_a_graph():
+    """The same plain op list run again and again: from its second run in a
+    row it is captured into a CUDA graph and replayed.  complex128: every run
+    equals the oracle bit for bit and counts its kernels; a changed angle
+    runs kernel by kernel again, and again matches the oracle."""
+    n = 14
+    basis, g = W.random_circuit(n, 5, 120)
+    full = W.basis_gates(n, basis)
+    full.extend(g)
+    with O.OracleState(n) as o:
+        o.run(full)
+        want = o.amplitudes()
+    with capi.State(n, capi.C128) as s:
+        counts = []
+        for rep in range(4):
+            s.set_basis(0)
+            l0 = s.launch_count()
+            s.run(full)
+            counts.append(s.launch_count() - l0)
+            assert bits_equal(s.amplitudes(), want), rep
+        assert len(set(counts)) == 1 and counts[0] > 0, counts
+        g2 = W.GateList()
+        g2.extend(full)
+        i = next(j for j, k in enumerate(g2.kinds) if k in W.PARAMETRIC)
+        g2.angles[i] += 0.25
+        with O.OracleState(n) as o:
+            o.run(g2)
+            want2 = o.amplitudes()
+        for rep in range(3):
+            s.set_basis(0)
+            s.run(g2)
+            assert bits_equal(s.amplitudes(), want2), rep
+
+
+def test_plain_graph_with_grover_barriers_is_deterministic():
+    """Phase flips and diffusions (whose sums the graph recomputes) inside a
+    replayed plain run: every replay equals the first, kernel-by-kernel run
+    bit for bit, and the FP64 oracle to complex64 rounding."""
+    n = 12
+    w = W.grover_workload(n, 9, iterations=6)
+    full = W.basis_gates(n, w.basis)
+    full.extend(w.qft)
+    full.extend(w.rounds)
+    with O.OracleState(n) as o:
+        o.run(full)
+        want = o.amplitudes()
+    with capi.State(n, capi.C64) as s:
+        first = None
+        for rep in range(4):
+            s.set_basis(0)
+            s.run(full)
+            a = s.amplitudes()
+            if first is None:
+                first = a
+            assert np.array_equal(a, first), rep
+        assert infidelity(first, want) < C64_INFID
+
+
 # ---- complex64 against the FP64 oracle ----------------------------------------
 
 @pytest.mark.parametrize("n,seed", [(12, 0), (16, 1), (18, 2)])
