@@ -94,9 +94,9 @@ typedef struct qcs_cuda_run_options {
  * exact bytes of the op list and on the options (and, for the learned
  * partitioner, the cost model and its current parameters); running the same
  * list again skips planning.  Any change (one angle) plans afresh.  A plain
- * run (one kernel per op) of a PHYSICAL state of at most 26 qubits and at
- * least 16 ops is captured into a CUDA graph when the same list runs twice in
- * a row, and replayed from then on (not while profiling).  This bit plans
+ * run (one kernel per op) of a state of at most 26 qubits and at least 16
+ * ops is captured into a CUDA graph when the same list runs twice in a row,
+ * and replayed from then on (not while profiling).  This bit plans
  * afresh every time, launches kernel by kernel, and leaves what is kept
  * untouched. */
 #define QCS_RUN_NO_PLAN_CACHE 1

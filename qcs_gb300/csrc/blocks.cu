@@ -341,19 +341,27 @@ constexpr size_t kPlanCacheMatBytes = 64u << 20;
 // circuits of short kernels whose launches, one per gate, take as long as
 // the kernels (a 20-qubit complex128 QFT phase: ~3 us of work).  The same op
 // list, byte for byte, is captured into a graph on its second run in a row
-// and replayed from then on: one graph launch per circuit.  PHYSICAL
-// semantics only (REFERENCE semantics swap the state's two buffers on the
-// host per gate).  The cached amplitude sum is reset before the capture and
-// before every replay, so the reductions the graph recorded are the ones a
-// fresh run would make.
+// and replayed from then on: one graph launch per circuit.  The cached
+// amplitude sum is reset before the capture and before every replay, so the
+// reductions the graph recorded are the ones a fresh run would make.
+// REFERENCE semantics sweep out of place and swap the state's two buffers
+// on the host after each sweep: a recording holds the buffers it started
+// from, so a list with an odd number of swaps needs one recording per
+// starting buffer (two at most), and each replay swaps the host's pointers
+// as the recorded run did.
 struct PlainGraph {
   std::vector<qcs_cuda_op> ops;
-  int seen = 0;                   // runs of this op list in a row
-  cudaGraphExec_t exec = nullptr;
-  long long launches = 0;         // kernels in the graph
-  int sum_valid_end = 0;          // the cached-sum flag after a run
+  int seen = 0;  // runs of this op list in a row
+  struct Rec {
+    void *start = nullptr;          // the buffer holding the state at the start
+    cudaGraphExec_t exec = nullptr;
+    bool swapped = false;           // the run ends in the other buffer
+    long long launches = 0;         // kernels in the graph
+    int sum_valid_end = 0;          // the cached-sum flag after a run
+  } rec[2];
   ~PlainGraph() {
-    if (exec) cudaGraphExecDestroy(exec);
+    for (Rec &r : rec)
+      if (r.exec) cudaGraphExecDestroy(r.exec);
   }
 };
 
@@ -478,6 +486,20 @@ static int run_plain(qcs_cuda_state *s, const qcs_cuda_op *ops, int count) {
   return QCS_CUDA_OK;
 }
 
+static int replay_plain(qcs_cuda_state *s, const PlainGraph::Rec &r) {
+  invalidate_sum(s);
+  int rc = check_cuda(cudaGraphLaunch(r.exec, s->stream), "plain graph launch");
+  if (rc) return rc;
+  if (r.swapped) {
+    void *t = s->vec;
+    s->vec = s->scratch;
+    s->scratch = t;
+  }
+  s->launches += r.launches;
+  s->sum_valid = r.sum_valid_end;
+  return QCS_CUDA_OK;
+}
+
 // The plain run through the kept graph (see PlainGraph).
 static int run_plain_kept(qcs_cuda_state *s, const qcs_cuda_op *ops, int count) {
   PlainGraph *g = s->plain_graph;
@@ -490,18 +512,16 @@ static int run_plain_kept(qcs_cuda_state *s, const qcs_cuda_op *ops, int count) 
     s->plain_graph = g;
   }
   g->seen++;
-  if (g->exec) {
-    invalidate_sum(s);
-    int rc = check_cuda(cudaGraphLaunch(g->exec, s->stream), "plain graph launch");
-    if (rc) return rc;
-    s->launches += g->launches;
-    s->sum_valid = g->sum_valid_end;
-    return QCS_CUDA_OK;
-  }
-  if (g->seen < 2) return run_plain(s, ops, count);
-  // second run in a row: record it, then launch the recording
+  for (const PlainGraph::Rec &r : g->rec)
+    if (r.exec && r.start == s->vec) return replay_plain(s, r);
+  PlainGraph::Rec *slot = !g->rec[0].exec ? &g->rec[0] : !g->rec[1].exec ? &g->rec[1] : nullptr;
+  if (g->seen < 2 || !slot) return run_plain(s, ops, count);
+  // second run in a row (from this buffer): record it, then launch the
+  // recording; the host-side swaps made while recording leave the pointers
+  // as the recorded run leaves them
   invalidate_sum(s);
   const long long l0 = s->launches;
+  void *start = s->vec, *start_scratch = s->scratch;
   int rc = check_cuda(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal),
                       "plain graph capture");
   if (rc) return rc;
@@ -509,20 +529,22 @@ static int run_plain_kept(qcs_cuda_state *s, const qcs_cuda_op *ops, int count) 
   cudaGraph_t graph = nullptr;
   const int rc_end = check_cuda(cudaStreamEndCapture(s->stream, &graph), "plain graph capture end");
   if (!rc) rc = rc_end;
-  if (!rc) rc = check_cuda(cudaGraphInstantiate(&g->exec, graph, 0), "plain graph instantiate");
+  cudaGraphExec_t exec = nullptr;
+  if (!rc) rc = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "plain graph instantiate");
   if (graph) cudaGraphDestroy(graph);
-  if (rc) {
-    s->launches = l0;
-    g->exec = nullptr;
-    return rc;
-  }
-  g->launches = s->launches - l0;
-  g->sum_valid_end = s->sum_valid;
-  s->launches = l0 + g->launches;
-  invalidate_sum(s);
-  rc = check_cuda(cudaGraphLaunch(g->exec, s->stream), "plain graph launch");
-  if (!rc) s->sum_valid = g->sum_valid_end;
-  return rc;
+  const long long n_launch = s->launches - l0;
+  const bool swapped = s->vec != start;
+  const int sum_end = s->sum_valid;
+  s->launches = l0;  // nothing ran while recording
+  s->vec = start;
+  s->scratch = start_scratch;
+  if (rc) return rc;
+  slot->start = start;
+  slot->exec = exec;
+  slot->swapped = swapped;
+  slot->launches = n_launch;
+  slot->sum_valid_end = sum_end;
+  return replay_plain(s, *slot);
 }
 
 int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda_run_options *opt) {
@@ -530,8 +552,7 @@ int run_ops(qcs_cuda_state *s, const qcs_cuda_op *ops, int count, const qcs_cuda
   if (rc) return rc;
   int k = opt ? opt->fusion_k : 0;
   if (k <= 1 || s->sem == QCS_CUDA_REFERENCE) {
-    const bool keep = !(opt && (opt->flags & QCS_RUN_NO_PLAN_CACHE)) &&
-                      s->sem == QCS_CUDA_PHYSICAL && !s->prof &&
+    const bool keep = !(opt && (opt->flags & QCS_RUN_NO_PLAN_CACHE)) && !s->prof &&
                       s->n <= kPlainGraphMaxQubits && count >= kPlainGraphMinOps;
     return keep ? run_plain_kept(s, ops, count) : run_plain(s, ops, count);
   }

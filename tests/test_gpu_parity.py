@@ -99,21 +99,27 @@ def test_reference_semantics_controlled_rule(prec):
                 np.testing.assert_allclose(s.amplitudes(), o.amplitudes(), atol=1e-5)
 
 
-def test_plain_runs_replay_from_a_graph():
+@pytest.mark.parametrize("sem,mode", [(capi.PHYSICAL, O.PHYSICAL), (capi.REFERENCE, O.COMPAT)])
+def test_plain_runs_replay_from_a_graph(sem, mode):
     """The same plain op list run again and again: from its second run in a
     row it is captured into a CUDA graph and replayed.  complex128: every run
     equals the oracle bit for bit and counts its kernels; a changed angle
-    runs kernel by kernel again, and again matches the oracle."""
+    runs kernel by kernel again, and again matches the oracle.  In REFERENCE
+    semantics every sweep swaps the state's two buffers; the list has an odd
+    number of sweeps, so successive runs start from alternate buffers and
+    each starting buffer gets a recording of its own."""
     n = 14
     basis, g = W.random_circuit(n, 5, 120)
     full = W.basis_gates(n, basis)
     full.extend(g)
-    with O.OracleState(n) as o:
+    if len(full) % 2 == 0:
+        full.add(W.I, 3)
+    with O.OracleState(n, mode) as o:
         o.run(full)
         want = o.amplitudes()
-    with capi.State(n, capi.C128) as s:
+    with capi.State(n, capi.C128, sem) as s:
         counts = []
-        for rep in range(4):
+        for rep in range(5):
             s.set_basis(0)
             l0 = s.launch_count()
             s.run(full)
@@ -124,10 +130,10 @@ def test_plain_runs_replay_from_a_graph():
         g2.extend(full)
         i = next(j for j, k in enumerate(g2.kinds) if k in W.PARAMETRIC)
         g2.angles[i] += 0.25
-        with O.OracleState(n) as o:
+        with O.OracleState(n, mode) as o:
             o.run(g2)
             want2 = o.amplitudes()
-        for rep in range(3):
+        for rep in range(4):
             s.set_basis(0)
             s.run(g2)
             assert bits_equal(s.amplitudes(), want2), rep
