@@ -260,7 +260,10 @@ __global__ void __launch_bounds__(kSweepThreads)
 // The reference's controlled sweep (src/q_gates.c:277-297), out of place:
 // every pair is copied, except that control=1 pairs get
 // lo := c_add(c_mul(g0,v0), c_mul(g1,v1)) and keep hi := v1.
-template <typename C>
+// FORM 1 (U01 = 0, e.g. CPHASE) and FORM 2 (U00 = 0, e.g. CNOT) leave out
+// the product with the zero entry: the values are the full formula's (that
+// product is +-0).
+template <typename C, int FORM>
 __global__ void __launch_bounds__(kSweepThreads)
     k_ctrl1q_reference(C *dst, const C *src, i64 npairs, int t, i64 cmask, Mat2<C> m) {
   const i64 nthr = (i64)gridDim.x * blockDim.x;
@@ -268,8 +271,42 @@ __global__ void __launch_bounds__(kSweepThreads)
   for (i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += nthr) {
     i64 lo = insert_zero(p, t);
     C v0 = src[lo], v1 = src[lo + tb];
-    dst[lo] = (lo & cmask) ? cadd(cmul(m.g[0], v0), cmul(m.g[1], v1)) : v0;
+    C x = v0;
+    if (lo & cmask)
+      x = FORM == 1 ? cmul(m.g[0], v0)
+          : FORM == 2 ? cmul(m.g[1], v1)
+                      : cadd(cmul(m.g[0], v0), cmul(m.g[1], v1));
+    dst[lo] = x;
     dst[lo + tb] = v1;
+  }
+}
+
+// REFERENCE semantics' one-qubit sweep, out of place, for a diagonal (FORM 1)
+// or exchange (FORM 2) 2x2: each output is one complex product, whose value
+// equals the full formula's (the other product is +-0).
+template <typename C, int FORM>
+__global__ void __launch_bounds__(kSweepThreads)
+    k_oop1q(C *dst, const C *src, i64 npairs, int t, Mat2<C> m) {
+  const i64 nthr = (i64)gridDim.x * blockDim.x;
+  const i64 tb = 1LL << t;
+  i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p < npairs; p += kUnroll * nthr) {
+    C v0[kUnroll], v1[kUnroll];
+    i64 lo[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      lo[u] = insert_zero(p + u * nthr, t);
+      if (p + u * nthr < npairs) {
+        v0[u] = src[lo[u]];
+        v1[u] = src[lo[u] + tb];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      if (p + u * nthr >= npairs) continue;
+      dst[lo[u]] = FORM == 1 ? cmul(m.g[0], v0[u]) : cmul(m.g[1], v1[u]);
+      dst[lo[u] + tb] = FORM == 1 ? cmul(m.g[3], v1[u]) : cmul(m.g[2], v0[u]);
+    }
   }
 }
 
@@ -304,9 +341,14 @@ static int apply_1q_t(qcs_cuda_state *s, const double m[8], int t) {
   C *v = (C *)s->vec;
   if (s->sem == QCS_CUDA_REFERENCE) {
     i64 np = s->size / 2;
+    const int gr = grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM);
     prof_begin(s);
-    k_dense1q<C><<<grid_for(np, kSweepThreads * kUnroll, d, kSweepBlocksPerSM), kSweepThreads, 0,
-                   s->stream>>>((C *)s->scratch, v, np, t, g);
+    if (is_zero(m + 2) && is_zero(m + 4))
+      k_oop1q<C, 1><<<gr, kSweepThreads, 0, s->stream>>>((C *)s->scratch, v, np, t, g);
+    else if (is_zero(m) && is_zero(m + 6))
+      k_oop1q<C, 2><<<gr, kSweepThreads, 0, s->stream>>>((C *)s->scratch, v, np, t, g);
+    else
+      k_dense1q<C><<<gr, kSweepThreads, 0, s->stream>>>((C *)s->scratch, v, np, t, g);
     int rc = launched(s, KC_DENSE1Q, 2 * Ns, "apply_1q");
     if (rc) return rc;
     swap_buffers(s);
@@ -357,8 +399,16 @@ static int apply_ctrl_t(qcs_cuda_state *s, const double m[8], int c, int t) {
   if (s->sem == QCS_CUDA_REFERENCE) {
     i64 np = s->size / 2;
     prof_begin(s);
-    k_ctrl1q_reference<C><<<grid_for(np, kSweepThreads, d, kSweepBlocksPerSM), kSweepThreads, 0,
-                            s->stream>>>((C *)s->scratch, v, np, t, cmask, g);
+    const int gr = grid_for(np, kSweepThreads, d, kSweepBlocksPerSM);
+    if (is_zero(m + 2))
+      k_ctrl1q_reference<C, 1><<<gr, kSweepThreads, 0, s->stream>>>((C *)s->scratch, v, np, t,
+                                                                     cmask, g);
+    else if (is_zero(m))
+      k_ctrl1q_reference<C, 2><<<gr, kSweepThreads, 0, s->stream>>>((C *)s->scratch, v, np, t,
+                                                                     cmask, g);
+    else
+      k_ctrl1q_reference<C, 0><<<gr, kSweepThreads, 0, s->stream>>>((C *)s->scratch, v, np, t,
+                                                                     cmask, g);
     int rc = launched(s, KC_CTRL1Q, 2 * Ns, "apply_controlled");
     if (rc) return rc;
     swap_buffers(s);
