@@ -624,6 +624,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // amplitudes: a producer warp instruction reads 256 contiguous bytes of each
 // of 2 columns, and the epilogue transposes 32 x 16 results through shared
 // memory, as in k_block_tc.
+// The other modes load and store the state evict-first (ld/st .cs): each
+// line is read once and written once, and so marked it leaves L2 before the
+// tile the bulk prefetch brought in ahead.  A block on high qubits spreads a
+// tile over 128 far-apart runs, where plain accesses evicted part of the
+// prefetched tile (at 26 qubits, qubits 19..25 read 9 % more DRAM bytes than
+// the state, qubits 7..13 2 %).  At 30 qubits the hint measured 3-9 % faster
+// on placements above qubit 12, and no change on qubits 7..13; in kLowMode
+// and in k_block_tc it measured no faster or slower, so those keep plain
+// accesses.
 template <int MODE, bool FUSED>
 __global__ void __launch_bounds__(Tc7::THREADS, 1)
     k_block_tc7(float2 *v, const __grid_constant__ TcGeom g, const uint4 *bimg, int renorm,
@@ -730,13 +739,13 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
           if constexpr (MODE == kPairMode) {
 #pragma unroll
             for (int e = 0; e < 8; e += 2) {
-              const float4 t = *reinterpret_cast<const float4 *>(src + blk_off[a + e]);
+              const float4 t = __ldcs(reinterpret_cast<const float4 *>(src + blk_off[a + e]));
               xc[b][i][e] = make_float2(t.x, t.y);
               xc[b][i][e + 1] = make_float2(t.z, t.w);
             }
           } else {
 #pragma unroll
-            for (int e = 0; e < 8; e++) xc[b][i][e] = src[blk_off[a + e]];
+            for (int e = 0; e < 8; e++) xc[b][i][e] = __ldcs(src + blk_off[a + e]);
           }
         }
       }
@@ -989,11 +998,11 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
         } else if constexpr (MODE == kPairMode) {
 #pragma unroll
           for (int q = 0; q < 16; q += 2)
-            *reinterpret_cast<float4 *>(dst + blk_off[16 * gq + q]) =
-                make_float4(re[q], im[q], re[q + 1], im[q + 1]);
+            __stcs(reinterpret_cast<float4 *>(dst + blk_off[16 * gq + q]),
+                   make_float4(re[q], im[q], re[q + 1], im[q + 1]));
         } else {
 #pragma unroll
-          for (int q = 0; q < 16; q++) dst[blk_off[16 * gq + q]] = make_float2(re[q], im[q]);
+          for (int q = 0; q < 16; q++) __stcs(dst + blk_off[16 * gq + q], make_float2(re[q], im[q]));
         }
       }
       tc_fence_before();
