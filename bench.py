@@ -528,7 +528,7 @@ def run_sweeps(args, dist):
     peak = measured_peaks()
     rng = np.random.default_rng(args.seed)
     out = {}
-    with capi.State(n, capi.C64) as s:
+    with capi.State(n, capi.C64) as s, ClockSampler() as clk:
         s.run(W.brick_circuit(n, 1, args.seed))  # a generic dense state (plain kernels)
         s.synchronize()
         u7, _ = np.linalg.qr(rng.normal(size=(128, 128)) + 1j * rng.normal(size=(128, 128)))
@@ -607,7 +607,7 @@ def run_sweeps(args, dist):
                          "kernel_ms": main_cls[1][1] / max(1, main_cls[1][0])}
     line = {"mode": "sweeps", "qubits": n, "state_bytes": int(Ns), "steps": args.steps,
             "warmup": args.warmup, "peak_hbm_gbs": peak["hbm_gbs"],
-            "peak_source": peak["source"], "sweeps": out}
+            "peak_source": peak["source"], "clocks": clk.summary(), "sweeps": out}
     print(json.dumps(line), flush=True)
 
 
