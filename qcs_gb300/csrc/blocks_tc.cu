@@ -621,9 +621,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 //   epilogue   reads Re and Im of 16 outputs at a time, both loads under
 //              one completion wait.
 // In kLowMode (the block is qubits 0..6) a column is 128 adjacent
-// amplitudes: a producer warp instruction reads 256 contiguous bytes of each
-// of 2 columns, and the epilogue transposes 32 x 16 results through shared
-// memory, as in k_block_tc.
+// amplitudes: a producer lane converts 4 adjacent amplitudes of a column (two
+// 16-byte loads, one 8-byte store per operand), so a warp's load pair reads
+// 256 contiguous bytes of each of 4 columns; the epilogue transposes 32 x 16
+// results through shared memory, as in k_block_tc.
 // The other modes load and store the state evict-first (ld/st .cs): each
 // line is read once and written once, and so marked it leaves L2 before the
 // tile the bulk prefetch brought in ahead.  A block on high qubits spreads a
@@ -709,9 +710,12 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
     const int p = tid - kTcEpiThreads;
     const int mc = p & (kTcM - 1);
     const int pw = p >> 5;
-    constexpr int LSTEPS = kTcM / (2 * S::PROD_WARPS);  // kLowMode: 2-column steps per chunk
+    // kLowMode: a warp instruction covers 4 columns, 8 lanes a column and 4
+    // adjacent amplitudes a lane (32 bytes: two 16-byte loads)
+    constexpr int LCOLS = 4;
+    constexpr int LSTEPS = kTcM / (LCOLS * S::PROD_WARPS);  // 4-column steps per chunk
     float2 xc[2][S::UPT][8];   // other modes: [chunk parity][unit][amplitude]
-    float4 xl[2][LSTEPS];      // kLowMode: [chunk parity][step]
+    float4 xl[2][LSTEPS][2];   // kLowMode: [chunk parity][step][amplitudes 0-1, 2-3]
     float partl[LSTEPS];       // kLowMode: per-step column norms over a tile
     const TileWalk w = tile_walk(g);
     const i64 nq = (i64)S::CHUNKS * w.count;  // chunks, an even number
@@ -727,9 +731,11 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
       if constexpr (MODE == kLowMode) {
 #pragma unroll
         for (int i = 0; i < LSTEPS; i++) {
-          const int m = pw * 2 * LSTEPS + 2 * i + (lane >> 4);
-          xl[b][i] = *reinterpret_cast<const float4 *>(v + base + col_off[m] + c * S::KC +
-                                                       2 * (lane & 15));
+          const int m = pw * LCOLS * LSTEPS + LCOLS * i + (lane >> 3);
+          const float4 *src = reinterpret_cast<const float4 *>(v + base + col_off[m] +
+                                                               c * S::KC + 4 * (lane & 7));
+          xl[b][i][0] = src[0];
+          xl[b][i][1] = src[1];
         }
       } else {
         const float2 *src = v + base + col_off[mc];
@@ -770,13 +776,16 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
       if constexpr (MODE == kLowMode) {
 #pragma unroll
         for (int i = 0; i < LSTEPS; i++) {
-          const float4 x = xl[b][i];
-          const int m = pw * 2 * LSTEPS + 2 * i + (lane >> 4);
-          uint32_t wd[4];
-          partl[i] += split2(make_float2(x.x, x.y), make_float2(x.z, x.w), wd);
-          const int off = sw64_offset(m, 2 * (lane & 15));
+          const float4 x0 = xl[b][i][0], x1 = xl[b][i][1];
+          const int m = pw * LCOLS * LSTEPS + LCOLS * i + (lane >> 3);
+          uint32_t w0[4], w1[4];
+          partl[i] += split2(make_float2(x0.x, x0.y), make_float2(x0.z, x0.w), w0);
+          partl[i] += split2(make_float2(x1.x, x1.y), make_float2(x1.z, x1.w), w1);
+          // 4 bf16 = 8 bytes inside one 16-byte swizzle chunk
+          const int off = sw64_offset(m, 4 * (lane & 7));
 #pragma unroll
-          for (int o = 0; o < 4; o++) *reinterpret_cast<uint32_t *>(st + o * S::CH_BYTES + off) = wd[o];
+          for (int o = 0; o < 4; o++)
+            *reinterpret_cast<uint2 *>(st + o * S::CH_BYTES + off) = make_uint2(w0[o], w1[o]);
         }
       } else {
 #pragma unroll
@@ -799,7 +808,7 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
       }
     };
     // the tile's column norms into slot it % 4: kLowMode sums each column's
-    // 16 lanes (fixed order); otherwise threads p and p + 128 hold the halves
+    // 8 lanes (fixed order); otherwise threads p and p + 128 hold the halves
     auto store_norms = [&](i64 it) {
       float *sq = colsq + (it % kSqSlots) * S::SQ_PARTS * kTcM;
       if constexpr (MODE == kLowMode) {
@@ -807,9 +816,9 @@ __global__ void __launch_bounds__(Tc7::THREADS, 1)
         for (int i = 0; i < LSTEPS; i++) {
           float x = partl[i];
 #pragma unroll
-          for (int o = 1; o < 16; o <<= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-          if ((lane & 15) == 0) {
-            const int m = pw * 2 * LSTEPS + 2 * i + (lane >> 4);
+          for (int o = 1; o < 8; o <<= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+          if ((lane & 7) == 0) {
+            const int m = pw * LCOLS * LSTEPS + LCOLS * i + (lane >> 3);
             sq[m] = x;
 #pragma unroll
             for (int h = 1; h < S::SQ_PARTS; h++) sq[h * kTcM + m] = 0.f;
